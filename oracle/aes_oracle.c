@@ -1,0 +1,481 @@
+/*
+ * aes_oracle.c -- CPU restatement of the AccelES two-stage low-bit Top-K SpMV path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for tests/, smoke() and bench.py's CPU legs.  The
+ * product library (acceles_gb300) never links or calls this file.
+ *
+ * Build with -ffp-contract=off: the FP32 gold sums are separately rounded multiply-then-add,
+ * which is what the GPU exact pass computes too.  References are to files of
+ * zhaijiaqi/AccelES.
+ */
+#include "aes_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* types.hpp:151-162: ULTRACSR_PACKET_SIZE = (512 - DIM_BOOL) / (B + 10 + 1), DIM_BOOL = 1. */
+int orc_packet_size(int bits) { return 511 / (bits + 11); }
+
+/* ---------------------------------------------------------------------------------------- */
+/* quantisers                                                                                */
+/* ---------------------------------------------------------------------------------------- */
+
+double orc_maxabs(const float* v, uint64_t n) {
+  /* quantify_util.py:24-26: max(abs(np.max(m)), abs(np.min(m))) over the dense matrix; the
+   * implicit zeros contribute |0|, so this is the max |v| over the stored values. */
+  double m = 0.0;
+  for (uint64_t i = 0; i < n; i++) {
+    double a = fabs((double)v[i]);
+    if (a > m) m = a;
+  }
+  return m;
+}
+
+int32_t orc_q_sym(double v, double m, int bits) {
+  /* quantify_util.py:21-27 (matrix) and :45-49 (vector): M = int((2^B-1)/2),
+   * clip(int32(round(M * (v / m))), -M-1, M) with numpy's round-half-to-even. */
+  int32_t M = ((1 << bits) - 1) / 2;
+  if (m == 0.0) return 0;
+  double x = v / m;
+  double y = (double)M * x;
+  double r = nearbyint(y); /* default rounding mode: to nearest, ties to even */
+  int32_t q = (int32_t)r;
+  if (q < -M - 1) q = -M - 1;
+  if (q > M) q = M;
+  return q;
+}
+
+int32_t orc_q_unsigned(double v, double m, int bits) {
+  int32_t M = (1 << bits) - 1;
+  if (m == 0.0) return 0;
+  double x = v / m;
+  double y = (double)M * x;
+  double r = nearbyint(y);
+  int32_t q = (int32_t)r;
+  if (q < 0) q = 0;
+  if (q > M) q = M;
+  return q;
+}
+
+int32_t orc_q_trunc(float v, int bits) {
+  /* quantize_utils.hpp:8-18.  q_temp = ap_fixed<32, B, AP_TRN_ZERO> (fpga_types.hpp:235, with
+   * B = QUANTIZE_B): (q_temp)(2^(B-2) * v) keeps 32-B fractional bits, truncating toward zero,
+   * and wraps the integer part (default AP_WRAP); to_int() truncates toward zero; the ap_int<B>
+   * cast wraps to B bits.  Parity unpinned: the ap_fixed sources are not available. */
+  int F = 32 - bits;
+  double x = (double)v * ldexp(1.0, bits - 2 + F); /* exact: power-of-two scaling */
+  double t = trunc(x);
+  int64_t X = (int64_t)t;
+  int32_t X32 = (int32_t)(uint32_t)(uint64_t)X;    /* 32-bit two's-complement wrap */
+  int32_t n = X32 / (int32_t)(1u << F);           /* C division truncates toward zero */
+  int32_t mask = (1 << bits) - 1;
+  int32_t half = 1 << (bits - 1);
+  int32_t w = ((n & mask) ^ half) - half;          /* ap_int<B> wrap */
+  return w;
+}
+
+int orc_quantize_query(const float* x, uint32_t cols, int bits, int quant, int qq, int32_t* out) {
+  if (qq == ORC_QQ_TRUNC) {
+    for (uint32_t j = 0; j < cols; j++) out[j] = orc_q_trunc(x[j], bits);
+    return 0;
+  }
+  if (quant == ORC_QUANT_UNSIGNED_ROW || quant == ORC_QUANT_UNSIGNED_GLOBAL) {
+    /* per-query unsigned scale; for UNSIGNED_GLOBAL this is quantify_vector(symmetric=False),
+     * whose clip bound -M-1 never binds on non-negative input */
+    double m = 0.0;
+    for (uint32_t j = 0; j < cols; j++) {
+      if (x[j] < 0.0f) return -1;
+      if ((double)x[j] > m) m = (double)x[j];
+    }
+    for (uint32_t j = 0; j < cols; j++) out[j] = orc_q_unsigned((double)x[j], m, bits);
+    return 0;
+  }
+  double m = orc_maxabs(x, cols);
+  for (uint32_t j = 0; j < cols; j++) out[j] = orc_q_sym((double)x[j], m, bits);
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* matrix quantisation + seeded empty-row rule                                               */
+/* ---------------------------------------------------------------------------------------- */
+
+static uint64_t splitmix64(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+uint64_t orc_quantize_matrix(const uint64_t* ptr, const uint32_t* col, const float* val,
+                             uint32_t rows, uint32_t cols, int bits, int quant, uint64_t seed,
+                             uint64_t* qptr, uint32_t* qcol, int32_t* qval, float* rowscale) {
+  uint64_t nnz = ptr[rows];
+  double gm = 0.0;
+  if (quant == ORC_QUANT_SYM_GLOBAL) {
+    gm = orc_maxabs(val, nnz);
+  } else {
+    if (quant == ORC_QUANT_UNSIGNED_GLOBAL) gm = orc_maxabs(val, nnz);
+    for (uint64_t e = 0; e < nnz; e++)
+      if (val[e] < 0.0f) return (uint64_t)-1;
+  }
+  uint64_t o = 0;
+  qptr[0] = 0;
+  for (uint32_t r = 0; r < rows; r++) {
+    uint64_t b = ptr[r], e_end = ptr[r + 1];
+    double m = gm;
+    if (quant == ORC_QUANT_UNSIGNED_ROW) {
+      m = 0.0;
+      for (uint64_t e = b; e < e_end; e++)
+        if ((double)val[e] > m) m = (double)val[e];
+      rowscale[r] = (float)(m / (double)((1 << bits) - 1));
+    }
+    uint64_t start = o;
+    for (uint64_t e = b; e < e_end; e++) {
+      int32_t q = (quant == ORC_QUANT_SYM_GLOBAL) ? orc_q_sym((double)val[e], m, bits)
+                                                  : orc_q_unsigned((double)val[e], m, bits);
+      /* UNSIGNED_GLOBAL: quantify_matrix(symmetric=False) clips to [-M-1, M]; with values >= 0
+       * that is orc_q_unsigned with the global scale */
+      if (q != 0) { /* matrix_to_coo keeps value != 0 only */
+        qcol[o] = col[e];
+        qval[o] = q;
+        o++;
+      }
+    }
+    if (o == start) { /* empty after quantisation: check_empty_rows puts a 1 in the row */
+      uint32_t c;
+      int32_t v = 1;
+      if (e_end > b) {
+        uint64_t best = b;
+        double ba = fabs((double)val[b]);
+        for (uint64_t e = b + 1; e < e_end; e++) {
+          double a = fabs((double)val[e]);
+          if (a > ba) { ba = a; best = e; }
+        }
+        c = col[best];
+        if (quant == ORC_QUANT_SYM_GLOBAL && val[best] < 0.0f) v = -1;
+      } else {
+        c = (uint32_t)(splitmix64(seed ^ (uint64_t)r) % (uint64_t)cols);
+      }
+      qcol[o] = c;
+      qval[o] = v;
+      o++;
+    }
+    qptr[r + 1] = o;
+  }
+  return o;
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* Ultra-CSR packets                                                                          */
+/* ---------------------------------------------------------------------------------------- */
+
+/* ap_uint<512>.range(hi, lo): bit i lives in byte i >> 3, bit i & 7. */
+static void put_bits(uint8_t* pkt, int pos, int width, uint32_t v) {
+  for (int b = 0; b < width; b++) {
+    int i = pos + b;
+    if ((v >> b) & 1u) pkt[i >> 3] |= (uint8_t)(1u << (i & 7));
+    else pkt[i >> 3] &= (uint8_t)~(1u << (i & 7));
+  }
+}
+
+static uint32_t get_bits(const uint8_t* pkt, int pos, int width) {
+  uint32_t v = 0;
+  for (int b = 0; b < width; b++) {
+    int i = pos + b;
+    v |= (uint32_t)((pkt[i >> 3] >> (i & 7)) & 1u) << b;
+  }
+  return v;
+}
+
+uint64_t orc_pack_ultracsr(const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                           uint32_t rows, int bits, uint32_t parts, uint8_t* out) {
+  const int P = orc_packet_size(bits);
+  if (parts == 0) parts = 1;
+  uint32_t slice = rows / parts;
+  uint64_t npk = 0;
+  uint32_t last_row = 0; /* host_spmv_ucsr.cpp:304: r_last = 0 before partition 0 */
+  for (uint32_t p = 0; p < parts; p++) {
+    uint32_t r0 = p * slice;
+    uint32_t r1 = (p == parts - 1) ? rows : (p + 1) * slice;
+    uint64_t e0 = qptr[r0], e1 = qptr[r1];
+    uint64_t n = e1 - e0;
+    uint64_t np = (n + (uint64_t)P - 1) / (uint64_t)P;
+    if (out) {
+      uint32_t r = r0;
+      for (uint64_t k = 0; k < np; k++) {
+        uint8_t* pkt = out + (npk + k) * 64;
+        memset(pkt, 0, 64);
+        for (int j = 0; j < P; j++) {
+          uint64_t e = e0 + k * (uint64_t)P + (uint64_t)j;
+          if (e >= e1) break; /* tail slots stay flag 0, col 0, val 0 (:407-411) */
+          while (qptr[r + 1] <= e) r++;
+          uint32_t flag = (r != last_row) ? 1u : 0u; /* :401-403 */
+          last_row = r;
+          put_bits(pkt, j, 1, flag);
+          put_bits(pkt, P + 10 * j, 10, qcol[e] & 0x3FFu);
+          put_bits(pkt, 11 * P + bits * j, bits, (uint32_t)qval[e] & ((1u << bits) - 1u));
+        }
+      }
+    } else if (n) {
+      /* keep last_row consistent for counting-only calls */
+      uint32_t r = r1 - 1;
+      while (qptr[r] == qptr[r + 1] && r > r0) r--;
+      last_row = r;
+    }
+    npk += np;
+  }
+  return npk;
+}
+
+void orc_xdecode(uint64_t flags, int P, uint32_t base, uint32_t* out) {
+  for (int i = 0; i < P; i++) {
+    uint64_t m = (i >= 63) ? ~0ull : ((2ull << i) - 1ull);
+    out[i] = base + (uint32_t)__builtin_popcountll(flags & m);
+  }
+}
+
+void orc_unpack_packet(const uint8_t* pkt, int bits, int is_signed, uint64_t* flags,
+                       uint32_t* cols, int32_t* vals) {
+  const int P = orc_packet_size(bits);
+  uint64_t f = 0;
+  for (int j = 0; j < P; j++) {
+    f |= (uint64_t)get_bits(pkt, j, 1) << j;
+    cols[j] = get_bits(pkt, P + 10 * j, 10);
+    uint32_t v = get_bits(pkt, 11 * P + bits * j, bits);
+    if (is_signed && (v >> (bits - 1))) vals[j] = (int32_t)v - (1 << bits);
+    else vals[j] = (int32_t)v;
+  }
+  *flags = f;
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* candidate pass                                                                             */
+/* ---------------------------------------------------------------------------------------- */
+
+void orc_int_scores(const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                    uint32_t rows, const int32_t* qq, int32_t* out) {
+  for (uint32_t r = 0; r < rows; r++) {
+    uint32_t acc = 0; /* int32 wrap-around arithmetic, as the int32 accumulator computes */
+    for (uint64_t e = qptr[r]; e < qptr[r + 1]; e++)
+      acc += (uint32_t)(qval[e] * qq[qcol[e]]);
+    out[r] = (int32_t)acc;
+  }
+}
+
+uint32_t orc_key_i32(int32_t s) { return (uint32_t)s ^ 0x80000000u; }
+
+uint32_t orc_key_f32(float f) {
+  if (f == 0.0f) f = 0.0f; /* -0 and +0 compare equal in sort_tuples */
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+void orc_cand_keys(const int32_t* scores, const float* rowscale, uint32_t rows, uint32_t* keys) {
+  for (uint32_t r = 0; r < rows; r++) {
+    if (rowscale) {
+      float s = (float)scores[r];
+      keys[r] = orc_key_f32(s * rowscale[r]);
+    } else {
+      keys[r] = orc_key_i32(scores[r]);
+    }
+  }
+}
+
+typedef struct {
+  uint64_t comp; /* key << 32 | row: (key desc, row desc) is descending comp */
+} comp_t;
+
+static int cmp_comp_desc(const void* a, const void* b) {
+  uint64_t x = ((const comp_t*)a)->comp, y = ((const comp_t*)b)->comp;
+  return (x > y) ? -1 : (x < y) ? 1 : 0;
+}
+
+uint32_t orc_select_split(const uint32_t* keys, uint32_t rows, uint32_t split, uint32_t ck,
+                          uint32_t* cand) {
+  uint32_t S = split <= 1 ? 1 : split;
+  uint32_t ntop = ck / S; /* int(APPROXIMATE_K / split_size), quantify_util.py:194 */
+  uint32_t slice = rows / S;
+  uint32_t outn = 0;
+  comp_t* buf = (comp_t*)malloc(sizeof(comp_t) * (rows ? rows : 1));
+  for (uint32_t p = 0; p < S; p++) {
+    uint32_t r0 = p * slice;
+    uint32_t r1 = (p == S - 1) ? rows : (p + 1) * slice; /* remainder on the last slice */
+    uint32_t n = r1 - r0;
+    for (uint32_t i = 0; i < n; i++)
+      buf[i].comp = ((uint64_t)keys[r0 + i] << 32) | (uint64_t)(r0 + i);
+    qsort(buf, n, sizeof(comp_t), cmp_comp_desc);
+    uint32_t take = n < ntop ? n : ntop;
+    for (uint32_t i = 0; i < take; i++) cand[outn++] = (uint32_t)(buf[i].comp & 0xFFFFFFFFu);
+  }
+  free(buf);
+  return outn;
+}
+
+void orc_gold_topk2(const uint32_t* coo_row, const uint32_t* coo_col, const int32_t* coo_val,
+                    uint64_t nnz, const int32_t* vec, int k, uint32_t* res_idx, int32_t* res_val) {
+  /* gold_algorithms.hpp:249-308 */
+  for (int i = 0; i < k; i++) { res_idx[i] = 0; res_val[i] = 0; }
+  if (nnz == 0) return;
+  uint32_t curr_row = coo_row[0];
+  int32_t curr_out = 0;
+  int curr_worst_idx = 0;
+  int32_t curr_worst_val = 0;
+  for (uint64_t i = 0; i < nnz; i++) {
+    uint32_t r = coo_row[i];
+    int32_t p = coo_val[i] * vec[coo_col[i]];
+    if (r == curr_row) {
+      curr_out += p;
+    } else {
+      if (curr_out >= curr_worst_val) {
+        res_idx[curr_worst_idx] = curr_row;
+        res_val[curr_worst_idx] = curr_out;
+        int wi = 0;
+        int32_t wv = res_val[0];
+        for (int j = 0; j < k; j++) {
+          if (res_val[j] < wv) { wi = j; wv = res_val[j]; }
+        }
+        curr_worst_idx = wi;
+        curr_worst_val = wv;
+      }
+      curr_row = r;
+      curr_out = p;
+    }
+  }
+  if (curr_out >= curr_worst_val) {
+    res_idx[curr_worst_idx] = curr_row;
+    res_val[curr_worst_idx] = curr_out;
+  }
+}
+
+void orc_gold_topk_f32(const uint32_t* coo_row, const uint32_t* coo_col, const float* coo_val,
+                       uint64_t nnz, const float* vec, int k, uint32_t* res_idx, float* res_val) {
+  /* gold_algorithms.hpp:189-247 */
+  for (int i = 0; i < k; i++) { res_idx[i] = 0; res_val[i] = 0.0f; }
+  if (nnz == 0) return;
+  uint32_t curr_row = coo_row[0];
+  float curr_out = 0.0f;
+  int curr_worst_idx = 0;
+  float curr_worst_val = 0.0f;
+  for (uint64_t i = 0; i < nnz; i++) {
+    uint32_t r = coo_row[i];
+    float p = coo_val[i] * vec[coo_col[i]];
+    if (r == curr_row) {
+      curr_out += p;
+    } else {
+      if (curr_out >= curr_worst_val) {
+        res_idx[curr_worst_idx] = curr_row;
+        res_val[curr_worst_idx] = curr_out;
+        int wi = 0;
+        float wv = res_val[0];
+        for (int j = 0; j < k; j++) {
+          if (res_val[j] < wv) { wi = j; wv = res_val[j]; }
+        }
+        curr_worst_idx = wi;
+        curr_worst_val = wv;
+      }
+      curr_row = r;
+      curr_out = p;
+    }
+  }
+  if (curr_out >= curr_worst_val) {
+    res_idx[curr_worst_idx] = curr_row;
+    res_val[curr_worst_idx] = curr_out;
+  }
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* exact pass and final order                                                                */
+/* ---------------------------------------------------------------------------------------- */
+
+void orc_rescore_f32(const uint64_t* ptr, const uint32_t* col, const float* val, const float* q,
+                     const uint32_t* rows, uint32_t n, float* out) {
+  for (uint32_t i = 0; i < n; i++) {
+    uint32_t r = rows[i];
+    float acc = 0.0f;
+    for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) {
+      float p = val[e] * q[col[e]];
+      acc = acc + p;
+    }
+    out[i] = acc;
+  }
+}
+
+void orc_scores_f64(const uint64_t* ptr, const uint32_t* col, const float* val, const float* q,
+                    uint32_t rows, double* out) {
+  for (uint32_t r = 0; r < rows; r++) {
+    double acc = 0.0;
+    for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) acc += (double)val[e] * (double)q[col[e]];
+    out[r] = acc;
+  }
+}
+
+typedef struct {
+  uint32_t idx;
+  float v;
+} tf_t;
+typedef struct {
+  uint32_t idx;
+  int32_t v;
+} ti_t;
+
+static int cmp_tf(const void* a, const void* b) {
+  const tf_t* x = (const tf_t*)a;
+  const tf_t* y = (const tf_t*)b;
+  if (x->v != y->v) return (x->v > y->v) ? -1 : 1;
+  return (x->idx > y->idx) ? -1 : (x->idx < y->idx) ? 1 : 0;
+}
+static int cmp_ti(const void* a, const void* b) {
+  const ti_t* x = (const ti_t*)a;
+  const ti_t* y = (const ti_t*)b;
+  if (x->v != y->v) return (x->v > y->v) ? -1 : 1;
+  return (x->idx > y->idx) ? -1 : (x->idx < y->idx) ? 1 : 0;
+}
+
+void orc_sort_tuples_f32(uint32_t n, uint32_t* idx, float* val) {
+  tf_t* t = (tf_t*)malloc(sizeof(tf_t) * (n ? n : 1));
+  for (uint32_t i = 0; i < n; i++) { t[i].idx = idx[i]; t[i].v = val[i]; }
+  qsort(t, n, sizeof(tf_t), cmp_tf);
+  for (uint32_t i = 0; i < n; i++) { idx[i] = t[i].idx; val[i] = t[i].v; }
+  free(t);
+}
+
+void orc_sort_tuples_i32(uint32_t n, uint32_t* idx, int32_t* val) {
+  ti_t* t = (ti_t*)malloc(sizeof(ti_t) * (n ? n : 1));
+  for (uint32_t i = 0; i < n; i++) { t[i].idx = idx[i]; t[i].v = val[i]; }
+  qsort(t, n, sizeof(ti_t), cmp_ti);
+  for (uint32_t i = 0; i < n; i++) { idx[i] = t[i].idx; val[i] = t[i].v; }
+  free(t);
+}
+
+uint32_t orc_two_stage(const uint64_t* ptr, const uint32_t* col, const float* val,
+                       const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                       const float* rowscale, uint32_t rows, uint32_t cols, int bits, int quant,
+                       int qq, uint32_t split, uint32_t ck, uint32_t k, const float* query,
+                       uint32_t* out_idx, float* out_score, uint32_t* cand, uint32_t* cand_n) {
+  int32_t* q = (int32_t*)malloc(sizeof(int32_t) * (cols ? cols : 1));
+  int32_t* s = (int32_t*)malloc(sizeof(int32_t) * (rows ? rows : 1));
+  uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * (rows ? rows : 1));
+  if (orc_quantize_query(query, cols, bits, quant, qq, q) != 0) {
+    free(q); free(s); free(keys);
+    *cand_n = 0;
+    return 0;
+  }
+  orc_int_scores(qptr, qcol, qval, rows, q, s);
+  orc_cand_keys(s, quant == ORC_QUANT_UNSIGNED_ROW ? rowscale : NULL, rows, keys);
+  uint32_t nc = orc_select_split(keys, rows, split, ck, cand);
+  *cand_n = nc;
+  float* sc = (float*)malloc(sizeof(float) * (nc ? nc : 1));
+  uint32_t* ix = (uint32_t*)malloc(sizeof(uint32_t) * (nc ? nc : 1));
+  memcpy(ix, cand, sizeof(uint32_t) * nc);
+  orc_rescore_f32(ptr, col, val, query, ix, nc, sc);
+  /* final order: sort_tuples on (row, fp32 score); -0 canonicalised like the device key */
+  for (uint32_t i = 0; i < nc; i++)
+    if (sc[i] == 0.0f) sc[i] = 0.0f;
+  orc_sort_tuples_f32(nc, ix, sc);
+  uint32_t nout = nc < k ? nc : k;
+  for (uint32_t i = 0; i < nout; i++) { out_idx[i] = ix[i]; out_score[i] = sc[i]; }
+  free(q); free(s); free(keys); free(sc); free(ix);
+  return nout;
+}

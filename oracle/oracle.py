@@ -1,0 +1,350 @@
+"""CPU oracle for the two-stage low-bit Top-K SpMV path (TEST INFRASTRUCTURE ONLY).
+
+This module is the checker.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU legs
+import it; the product package ``acceles_gb300`` never does.  It wraps ``aes_oracle.c`` (a plain
+C restatement of the reference path, built into ``oracle/_build/liboracle.so``) and, when it was
+compiled on this machine, ``oracle/_ref/libaes_ref.so`` (the reference's own gold code from
+zhaijiaqi/AccelES, see ``oracle/Makefile``).
+
+Reference anchors (files of zhaijiaqi/AccelES):
+  quantify_matrix / quantify_vector   src/resources/python/quantify/quantify_util.py:8-49
+  split_approximate                   src/resources/python/quantify/quantify_util.py:173-196
+  spmv_coo_gold_top_k(_2)             src/fpga/src/gold_algorithms/gold_algorithms.hpp:189-308
+  sort_tuples                         src/common/utils/evaluation_utils.hpp:40-62
+  Ultra-CSR packet layout             src/fpga/src/ip/fpga_utils.hpp:317-527, types.hpp:151-162
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libaes_ref.so")
+
+QUANT_SYM_GLOBAL = 0
+QUANT_UNSIGNED_ROW = 1
+QUANT_UNSIGNED_GLOBAL = 2
+QQ_NUMPY = 0
+QQ_TRUNC = 1
+
+_lib = None
+_ref = None
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(ref: bool = False) -> None:
+    """Compile the oracle (and, if asked and the reference sources exist, oracle/_ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_packet_size.restype = ctypes.c_int
+        L.orc_maxabs.restype = ctypes.c_double
+        L.orc_maxabs.argtypes = [_f32p, ctypes.c_uint64]
+        L.orc_q_sym.restype = ctypes.c_int32
+        L.orc_q_sym.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.orc_q_unsigned.restype = ctypes.c_int32
+        L.orc_q_unsigned.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.orc_q_trunc.restype = ctypes.c_int32
+        L.orc_q_trunc.argtypes = [ctypes.c_float, ctypes.c_int]
+        L.orc_quantize_query.restype = ctypes.c_int
+        L.orc_quantize_query.argtypes = [_f32p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, _i32p]
+        L.orc_quantize_matrix.restype = ctypes.c_uint64
+        L.orc_quantize_matrix.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _u64p,
+                                          _u32p, _i32p, _f32p]
+        L.orc_pack_ultracsr.restype = ctypes.c_uint64
+        L.orc_pack_ultracsr.argtypes = [_u64p, _u32p, _i32p, ctypes.c_uint32, ctypes.c_int,
+                                        ctypes.c_uint32, _u8p]
+        L.orc_xdecode.restype = None
+        L.orc_xdecode.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_uint32, _u32p]
+        L.orc_unpack_packet.restype = None
+        L.orc_unpack_packet.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _u64p, _u32p, _i32p]
+        L.orc_int_scores.restype = None
+        L.orc_int_scores.argtypes = [_u64p, _u32p, _i32p, ctypes.c_uint32, _i32p, _i32p]
+        L.orc_key_i32.restype = ctypes.c_uint32
+        L.orc_key_i32.argtypes = [ctypes.c_int32]
+        L.orc_key_f32.restype = ctypes.c_uint32
+        L.orc_key_f32.argtypes = [ctypes.c_float]
+        L.orc_cand_keys.restype = None
+        L.orc_cand_keys.argtypes = [_i32p, _f32p, ctypes.c_uint32, _u32p]
+        L.orc_select_split.restype = ctypes.c_uint32
+        L.orc_select_split.argtypes = [_u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                       _u32p]
+        L.orc_gold_topk2.restype = None
+        L.orc_gold_topk2.argtypes = [_u32p, _u32p, _i32p, ctypes.c_uint64, _i32p, ctypes.c_int,
+                                     _u32p, _i32p]
+        L.orc_gold_topk_f32.restype = None
+        L.orc_gold_topk_f32.argtypes = [_u32p, _u32p, _f32p, ctypes.c_uint64, _f32p,
+                                        ctypes.c_int, _u32p, _f32p]
+        L.orc_rescore_f32.restype = None
+        L.orc_rescore_f32.argtypes = [_u64p, _u32p, _f32p, _f32p, _u32p, ctypes.c_uint32, _f32p]
+        L.orc_scores_f64.restype = None
+        L.orc_scores_f64.argtypes = [_u64p, _u32p, _f32p, _f32p, ctypes.c_uint32, _f64p]
+        L.orc_sort_tuples_f32.restype = None
+        L.orc_sort_tuples_f32.argtypes = [ctypes.c_uint32, _u32p, _f32p]
+        L.orc_sort_tuples_i32.restype = None
+        L.orc_sort_tuples_i32.argtypes = [ctypes.c_uint32, _u32p, _i32p]
+        L.orc_two_stage.restype = ctypes.c_uint32
+        L.orc_two_stage.argtypes = [_u64p, _u32p, _f32p, _u64p, _u32p, _i32p, _f32p,
+                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, _f32p, _u32p, _f32p, _u32p, _u32p]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own gold code compiled on this machine, or None."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        try:
+            R = ctypes.CDLL(REF_PATH)
+        except OSError:
+            return None
+        R.ref_gold_topk2_i32.restype = None
+        R.ref_gold_topk2_i32.argtypes = [_u32p, _u32p, _i32p, ctypes.c_uint64, _i32p,
+                                         ctypes.c_int, _u32p, _i32p]
+        R.ref_gold_topk_f32.restype = None
+        R.ref_gold_topk_f32.argtypes = [_u32p, _u32p, _f32p, ctypes.c_uint64, _f32p,
+                                        ctypes.c_int, _u32p, _f32p]
+        R.ref_gold4_f32.restype = None
+        R.ref_gold4_f32.argtypes = [_u32p, _u32p, _f32p, ctypes.c_uint64, _f32p,
+                                    ctypes.c_uint32, _f32p]
+        R.ref_sort_tuples_f32.restype = None
+        R.ref_sort_tuples_f32.argtypes = [ctypes.c_uint32, _u32p, _f32p]
+        R.ref_sort_tuples_i32.restype = None
+        R.ref_sort_tuples_i32.argtypes = [ctypes.c_uint32, _u32p, _i32p]
+        R.ref_sort_pr_f32.restype = None
+        R.ref_sort_pr_f32.argtypes = [ctypes.c_uint32, _f32p, _u32p]
+        _ref = R
+    return _ref
+
+
+# ---------------------------------------------------------------------------------------------
+# numpy-facing wrappers
+# ---------------------------------------------------------------------------------------------
+
+def packet_size(bits: int) -> int:
+    return lib().orc_packet_size(bits)
+
+
+def csr_from_coo(rows, row, col, val):
+    """Stable (row, col) sort -> (ptr u64, col u32, val f32)."""
+    row = np.asarray(row, np.uint32)
+    col = np.asarray(col, np.uint32)
+    val = np.asarray(val, np.float32)
+    order = np.lexsort((col, row))
+    row, col, val = row[order], col[order], val[order]
+    ptr = np.zeros(rows + 1, np.uint64)
+    np.add.at(ptr, row.astype(np.int64) + 1, 1)
+    ptr = np.cumsum(ptr).astype(np.uint64)
+    return ptr, np.ascontiguousarray(col), np.ascontiguousarray(val)
+
+
+def quantize_query(x, bits, quant=QUANT_SYM_GLOBAL, qq=QQ_NUMPY):
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros(x.shape[0], np.int32)
+    rc = lib().orc_quantize_query(_p(x, _f32p), x.shape[0], bits, quant, qq, _p(out, _i32p))
+    if rc != 0:
+        raise ValueError("unsigned query quantiser needs non-negative entries")
+    return out
+
+
+def quantize_matrix(ptr, col, val, rows, cols, bits, quant=QUANT_SYM_GLOBAL, seed=0):
+    nnz = int(ptr[-1])
+    qptr = np.zeros(rows + 1, np.uint64)
+    qcol = np.zeros(nnz + rows + 1, np.uint32)
+    qval = np.zeros(nnz + rows + 1, np.int32)
+    rs = np.zeros(max(rows, 1), np.float32)
+    n = lib().orc_quantize_matrix(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                                  bits, quant, seed, _p(qptr, _u64p), _p(qcol, _u32p),
+                                  _p(qval, _i32p), _p(rs, _f32p))
+    if n == (1 << 64) - 1:
+        raise ValueError("unsigned quantiser needs non-negative matrix values")
+    return qptr, qcol[:n].copy(), qval[:n].copy(), (rs[:rows].copy() if quant == QUANT_UNSIGNED_ROW else None)
+
+
+def pack_ultracsr(qptr, qcol, qval, rows, bits, parts=32):
+    n = lib().orc_pack_ultracsr(_p(qptr, _u64p), _p(qcol, _u32p), _p(qval, _i32p), rows, bits,
+                                parts, None)
+    out = np.zeros(max(int(n), 1) * 64, np.uint8)
+    lib().orc_pack_ultracsr(_p(qptr, _u64p), _p(qcol, _u32p), _p(qval, _i32p), rows, bits, parts,
+                            _p(out, _u8p))
+    return out[: int(n) * 64].reshape(int(n), 64)
+
+
+def xdecode(flags: int, P: int, base: int = 0):
+    out = np.zeros(P, np.uint32)
+    lib().orc_xdecode(flags, P, base, _p(out, _u32p))
+    return out
+
+
+def unpack_packet(pkt, bits, is_signed=True):
+    pkt = np.ascontiguousarray(pkt, np.uint8)
+    P = packet_size(bits)
+    f = np.zeros(1, np.uint64)
+    c = np.zeros(P, np.uint32)
+    v = np.zeros(P, np.int32)
+    lib().orc_unpack_packet(_p(pkt, _u8p), bits, 1 if is_signed else 0, _p(f, _u64p),
+                            _p(c, _u32p), _p(v, _i32p))
+    return int(f[0]), c, v
+
+
+def int_scores(qptr, qcol, qval, rows, qq):
+    qq = np.ascontiguousarray(qq, np.int32)
+    out = np.zeros(rows, np.int32)
+    lib().orc_int_scores(_p(qptr, _u64p), _p(qcol, _u32p), _p(qval, _i32p), rows, _p(qq, _i32p),
+                         _p(out, _i32p))
+    return out
+
+
+def cand_keys(scores, rowscale=None):
+    scores = np.ascontiguousarray(scores, np.int32)
+    keys = np.zeros(scores.shape[0], np.uint32)
+    rs = None if rowscale is None else np.ascontiguousarray(rowscale, np.float32)
+    lib().orc_cand_keys(_p(scores, _i32p), None if rs is None else _p(rs, _f32p),
+                        scores.shape[0], _p(keys, _u32p))
+    return keys
+
+
+def key_f32(x: float) -> int:
+    return lib().orc_key_f32(x)
+
+
+def select_split(keys, split, ck):
+    keys = np.ascontiguousarray(keys, np.uint32)
+    out = np.zeros(max(ck, 1), np.uint32)
+    n = lib().orc_select_split(_p(keys, _u32p), keys.shape[0], split, ck, _p(out, _u32p))
+    return out[:n].copy()
+
+
+def gold_topk2(coo_row, coo_col, coo_val, vec, k, use_ref=False):
+    L = ref_lib() if use_ref else lib()
+    coo_row = np.ascontiguousarray(coo_row, np.uint32)
+    coo_col = np.ascontiguousarray(coo_col, np.uint32)
+    coo_val = np.ascontiguousarray(coo_val, np.int32)
+    vec = np.ascontiguousarray(vec, np.int32)
+    idx = np.zeros(k, np.uint32)
+    val = np.zeros(k, np.int32)
+    fn = L.ref_gold_topk2_i32 if use_ref else L.orc_gold_topk2
+    fn(_p(coo_row, _u32p), _p(coo_col, _u32p), _p(coo_val, _i32p), coo_row.shape[0],
+       _p(vec, _i32p), k, _p(idx, _u32p), _p(val, _i32p))
+    return idx, val
+
+
+def gold_topk_f32(coo_row, coo_col, coo_val, vec, k, use_ref=False):
+    L = ref_lib() if use_ref else lib()
+    coo_row = np.ascontiguousarray(coo_row, np.uint32)
+    coo_col = np.ascontiguousarray(coo_col, np.uint32)
+    coo_val = np.ascontiguousarray(coo_val, np.float32)
+    vec = np.ascontiguousarray(vec, np.float32)
+    idx = np.zeros(k, np.uint32)
+    val = np.zeros(k, np.float32)
+    fn = L.ref_gold_topk_f32 if use_ref else L.orc_gold_topk_f32
+    fn(_p(coo_row, _u32p), _p(coo_col, _u32p), _p(coo_val, _f32p), coo_row.shape[0],
+       _p(vec, _f32p), k, _p(idx, _u32p), _p(val, _f32p))
+    return idx, val
+
+
+def rescore_f32(ptr, col, val, q, rows_sel):
+    q = np.ascontiguousarray(q, np.float32)
+    rows_sel = np.ascontiguousarray(rows_sel, np.uint32)
+    out = np.zeros(rows_sel.shape[0], np.float32)
+    lib().orc_rescore_f32(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), _p(q, _f32p),
+                          _p(rows_sel, _u32p), rows_sel.shape[0], _p(out, _f32p))
+    return out
+
+
+def scores_f64(ptr, col, val, q, rows):
+    q = np.ascontiguousarray(q, np.float32)
+    out = np.zeros(rows, np.float64)
+    lib().orc_scores_f64(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), _p(q, _f32p), rows,
+                         _p(out, _f64p))
+    return out
+
+
+def sort_tuples_f32(idx, val, use_ref=False):
+    idx = np.array(idx, np.uint32)
+    val = np.array(val, np.float32)
+    L = ref_lib() if use_ref else lib()
+    fn = L.ref_sort_tuples_f32 if use_ref else L.orc_sort_tuples_f32
+    fn(idx.shape[0], _p(idx, _u32p), _p(val, _f32p))
+    return idx, val
+
+
+class Matrix:
+    """A synthetic matrix in the three forms the oracle needs (FP32 CSR, quantised CSR,
+    Ultra-CSR packets)."""
+
+    def __init__(self, rows, cols, ptr, col, val, bits, quant=QUANT_SYM_GLOBAL, seed=0,
+                 parts=32):
+        self.rows, self.cols, self.bits, self.quant = int(rows), int(cols), int(bits), int(quant)
+        self.ptr = np.ascontiguousarray(ptr, np.uint64)
+        self.col = np.ascontiguousarray(col, np.uint32)
+        self.val = np.ascontiguousarray(val, np.float32)
+        self.qptr, self.qcol, self.qval, self.rowscale = quantize_matrix(
+            self.ptr, self.col, self.val, self.rows, self.cols, self.bits, self.quant, seed)
+        self.parts = parts
+
+    def packets(self):
+        return pack_ultracsr(self.qptr, self.qcol, self.qval, self.rows, self.bits, self.parts)
+
+    def int_scores(self, query_f32, qq=QQ_NUMPY):
+        q = quantize_query(query_f32, self.bits, self.quant, qq)
+        return int_scores(self.qptr, self.qcol, self.qval, self.rows, q)
+
+    def keys(self, query_f32, qq=QQ_NUMPY):
+        return cand_keys(self.int_scores(query_f32, qq),
+                         self.rowscale if self.quant == QUANT_UNSIGNED_ROW else None)
+
+    def two_stage(self, query_f32, split, ck, k, qq=QQ_NUMPY):
+        q = np.ascontiguousarray(query_f32, np.float32)
+        oi = np.zeros(max(k, 1), np.uint32)
+        os_ = np.zeros(max(k, 1), np.float32)
+        cand = np.zeros(max(ck, 1), np.uint32)
+        cn = np.zeros(1, np.uint32)
+        rs = self.rowscale if self.rowscale is not None else np.zeros(1, np.float32)
+        n = lib().orc_two_stage(_p(self.ptr, _u64p), _p(self.col, _u32p), _p(self.val, _f32p),
+                                _p(self.qptr, _u64p), _p(self.qcol, _u32p),
+                                _p(self.qval, _i32p), _p(rs, _f32p), self.rows, self.cols,
+                                self.bits, self.quant, qq, split, ck, k, _p(q, _f32p),
+                                _p(oi, _u32p), _p(os_, _f32p), _p(cand, _u32p), _p(cn, _u32p))
+        return oi[:n].copy(), os_[:n].copy(), cand[: int(cn[0])].copy()
+
+
+# ---------------------------------------------------------------------------------------------
+# numpy restatements (cross-checks of the C code against the Python reference's arithmetic)
+# ---------------------------------------------------------------------------------------------
+
+def np_quantify_vector(v, B, symmetric=True):
+    """quantify_util.py:31-49 on a float64 copy."""
+    v = np.array(v, np.float64)
+    M = 2 ** B - 1
+    if symmetric:
+        M = int(M / 2)
+    m = max(abs(np.max(v)), abs(np.min(v)))
+    v /= m
+    return np.clip(np.int32(np.round(M * v)), int(-M) - 1, int(M))
