@@ -1,0 +1,769 @@
+// aes_engine.cu -- the device-resident Top-K SpMV engine behind the C ABI of include/acceles.h.
+//
+// One handle = one matrix resident in HBM (Ultra-CSR tiles + FP32 CSR) plus per-batch buffers.
+// A run enqueues, on the handle's stream:
+//   k_quantize -> k_cand_plain(sample tiles) -> k_threshold -> k_cand_plain(all tiles, filter)
+//   -> k_select -> k_final
+// and afterwards repairs, on the exact slow path, any query whose sample threshold missed or
+// whose survivor buffer overflowed (status bits).  Reference host API replaced:
+// struct SpMV, src/fpga/src/host_spmv_ucsr.cpp:134-829 (zhaijiaqi/AccelES).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "acceles.h"
+#include "aes_host.hpp"
+#include "aes_kernels.cuh"
+
+namespace aes {
+const char* last_error_cstr();
+
+#define AES_CK(x)                                                                            \
+  do {                                                                                       \
+    cudaError_t e_ = (x);                                                                    \
+    if (e_ != cudaSuccess) return ::aes::fail(AES_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+using namespace dev;
+
+typedef void (*PlainKernel)(PlainArgs);
+
+template <int B, bool SGN>
+static PlainKernel plain_kernel(int mode) {
+  switch (mode) {
+    case MODE_FILTER: return k_cand_plain<B, SGN, MODE_FILTER>;
+    case MODE_SAMPLE: return k_cand_plain<B, SGN, MODE_SAMPLE>;
+    default: return k_cand_plain<B, SGN, MODE_ALL>;
+  }
+}
+
+static PlainKernel pick_plain(int bits, bool sgn, int mode) {
+  switch (bits) {
+    case 4: return sgn ? plain_kernel<4, true>(mode) : plain_kernel<4, false>(mode);
+    case 6: return sgn ? plain_kernel<6, true>(mode) : plain_kernel<6, false>(mode);
+    default: return sgn ? plain_kernel<8, true>(mode) : plain_kernel<8, false>(mode);
+  }
+}
+
+// P(Bin(n, f) >= r) in log space
+static double binom_tail(uint32_t n, double f, uint32_t r) {
+  if (r == 0) return 1.0;
+  if (r > n) return 0.0;
+  if (f <= 0.0) return 0.0;
+  if (f >= 1.0) return 1.0;
+  double lf = std::log(f), l1f = std::log1p(-f), s = 0.0;
+  for (uint32_t k = r; k <= n; k++) {
+    double lt = std::lgamma((double)n + 1) - std::lgamma((double)k + 1) -
+                std::lgamma((double)(n - k) + 1) + k * lf + (n - k) * l1f;
+    s += std::exp(lt);
+  }
+  return s;
+}
+
+struct Engine {
+  aes_params prm{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int sm_count = 0;
+
+  uint32_t rows = 0, cols = 0, bits = 0, quant = 0, P = 0;
+  uint64_t nnz = 0, qnnz = 0, packets = 0, tiles = 0;
+  bool sgn = true;
+
+  uint4* d_tiles = nullptr;
+  uint32_t* d_tile_rowbase = nullptr;
+  float* d_rowscale = nullptr;
+  uint32_t* d_csr_ptr = nullptr;
+  uint16_t* d_csr_col = nullptr;
+  float* d_csr_val = nullptr;
+
+  uint32_t ss = 1, n_sample_tiles = 0, n_sample_rows = 0;
+  uint32_t* d_sample_first = nullptr;
+  uint32_t* d_part_sample_begin = nullptr;
+  uint32_t* d_part_r = nullptr;
+
+  uint32_t split = 1, slice = 0, ntop = 0, nslots = 0, npow2 = 0, ck_eff = 0, cap = 0;
+
+  uint32_t maxB = 1, ld32 = 0, ld8 = 0;
+  float* d_q32 = nullptr;
+  int8_t* d_q8 = nullptr;
+  uint32_t* d_sample_keys = nullptr;
+  uint32_t* d_thr = nullptr;
+  uint32_t* d_cnt = nullptr;
+  uint2* d_surv = nullptr;
+  uint32_t* d_cand = nullptr;
+  uint32_t* d_cand_key = nullptr;
+  uint32_t* d_status = nullptr;
+  uint32_t* d_out_idx = nullptr;
+  float* d_out_score = nullptr;
+  uint32_t* d_allkeys = nullptr;
+
+  float* h_q32 = nullptr;         // pinned staging of queries
+  uint32_t* h_status = nullptr;   // pinned
+  uint32_t nq_loaded = 0;
+  uint32_t last_nq = 0, last_k = 0;
+  bool last_from_device = false;
+  const float* last_q32 = nullptr;   // query buffer of the last run
+  uint32_t* last_idx = nullptr;      // device outputs of the last run
+  float* last_score = nullptr;
+  cudaStream_t last_stream = nullptr;
+  bool ran = false;
+
+  int plain_grid = 0;
+  size_t plain_smem = 0, final_smem = 0;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+
+  ~Engine() { release(); }
+
+  void release() {
+    if (device >= 0) cudaSetDevice(device);
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    if (h_q32) cudaFreeHost(h_q32);
+    if (h_status) cudaFreeHost(h_status);
+    h_q32 = nullptr;
+    h_status = nullptr;
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+    ev0 = ev1 = nullptr;
+    stream = nullptr;
+  }
+
+  template <class T>
+  int dalloc(T** p, size_t n) {
+    size_t b = std::max<size_t>(n * sizeof(T), 16);
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(AES_ERR_NOMEM, std::string("cudaMalloc refused: ") + cudaGetErrorString(e));
+    }
+    allocs.push_back(q);
+    bytes += b;
+    *p = reinterpret_cast<T*>(q);
+    return AES_OK;
+  }
+
+  int build(const HostCSR& m, const aes_params& p);
+  int enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
+              cudaStream_t s);
+  int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
+             uint32_t* repaired);
+  int run_plain(int mode, uint32_t q, cudaStream_t s);
+};
+
+int Engine::build(const HostCSR& m, const aes_params& p) {
+  prm = p;
+  device = p.device;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(AES_ERR_NODEV, "no CUDA device");
+  }
+  if (device < 0 || device >= ndev) return fail(AES_ERR_INVALID, "device ordinal out of range");
+  AES_CK(cudaSetDevice(device));
+  AES_CK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+  AES_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  AES_CK(cudaEventCreate(&ev0));
+  AES_CK(cudaEventCreate(&ev1));
+
+  rows = m.rows;
+  cols = m.cols;
+  bits = p.bits;
+  quant = p.quant;
+  sgn = (quant == AES_QUANT_SYM_GLOBAL);
+  nnz = m.ptr[rows];
+  if (nnz >= 0xFFFFFFFFull) return fail(AES_ERR_UNSUPPORTED, "nnz must be below 2^32");
+
+  PackedMatrix pm;
+  int rc = quantize_and_pack(m, p, &pm);
+  if (rc) return rc;
+  P = pm.P;
+  qnnz = pm.qnnz;
+  packets = pm.packets;
+  tiles = pm.tiles;
+  if (tiles >= 0xFFFFFFFFull) return fail(AES_ERR_UNSUPPORTED, "matrix too large");
+
+  // ---- selection geometry ----------------------------------------------------------------
+  split = p.split <= 1 ? 1 : p.split;
+  slice = rows / split;
+  ntop = p.ck / split;
+  nslots = split * ntop;
+  npow2 = 1;
+  while (npow2 < nslots) npow2 <<= 1;
+  ck_eff = 0;
+  std::vector<uint32_t> prow(split);
+  for (uint32_t q = 0; q < split; q++) {
+    uint32_t r0 = q * slice, r1 = (q == split - 1) ? rows : (q + 1) * slice;
+    prow[q] = r1 - r0;
+    ck_eff += std::min(ntop, prow[q]);
+  }
+
+  // ---- sample tiles -------------------------------------------------------------------------
+  if (p.sample_stride) ss = p.sample_stride;
+  else ss = tiles <= 64 ? 1 : 64;
+  n_sample_tiles = (uint32_t)((tiles + ss - 1) / ss);
+  auto owned_begin = [&](uint64_t t) -> uint64_t {
+    if (t >= tiles) return rows;
+    return t == 0 ? 0 : (uint64_t)pm.tile_rowbase[t] + 1;
+  };
+  std::vector<uint32_t> sample_first(n_sample_tiles);
+  std::vector<uint64_t> s_begin(n_sample_tiles), s_end(n_sample_tiles);
+  uint64_t pre = 0;
+  for (uint32_t s = 0; s < n_sample_tiles; s++) {
+    uint64_t t = (uint64_t)s * ss;
+    uint64_t b = owned_begin(t), e = std::max(b, owned_begin(t + 1));
+    s_begin[s] = b;
+    s_end[s] = e;
+    sample_first[s] = (uint32_t)(b - pre);
+    pre += e - b;
+  }
+  n_sample_rows = (uint32_t)pre;
+  // sample index range of each partition
+  std::vector<uint32_t> part_begin(split + 1, 0);
+  {
+    uint32_t s = 0;
+    uint64_t idx = 0;  // sample rows before s_begin[s]
+    for (uint32_t q = 0; q <= split; q++) {
+      uint64_t rb = (q == split) ? rows : (uint64_t)q * slice;
+      // count sample rows with row < rb
+      while (s < n_sample_tiles && s_end[s] <= rb) { idx += s_end[s] - s_begin[s]; s++; }
+      uint64_t c = idx;
+      if (s < n_sample_tiles && s_begin[s] < rb) c += rb - s_begin[s];
+      part_begin[q] = (uint32_t)c;
+    }
+    part_begin[split] = n_sample_rows;
+  }
+  std::vector<uint32_t> part_r(split);
+  size_t cap_need = 1024;
+  for (uint32_t q = 0; q < split; q++) {
+    uint32_t ns = part_begin[q + 1] - part_begin[q];
+    double f = prow[q] ? (double)ns / (double)prow[q] : 1.0;
+    uint32_t n1 = ntop ? ntop - 1 : 0;
+    uint32_t r = 1;
+    if (f >= 1.0) r = std::max<uint32_t>(ntop, 1);
+    else {
+      r = (uint32_t)std::floor(n1 * f);
+      while (r <= n1 && binom_tail(n1, f, r) > 1e-12) r++;
+      r = std::max<uint32_t>(r, 1);
+    }
+    part_r[q] = r;
+    double expect = f > 0 ? (double)r / f : (double)prow[q];
+    size_t c = (size_t)std::min<double>((double)prow[q], 4.0 * expect + 4.0 * ntop + 1024.0);
+    cap_need = std::max(cap_need, c);
+  }
+  cap = (uint32_t)std::min<size_t>(cap_need, (size_t)rows);
+  if (cap == 0) cap = 1;
+
+  // ---- memory plan and admission ------------------------------------------------------------
+  maxB = std::max<uint32_t>(p.max_batch, 1);
+  ld32 = (cols + 3) & ~3u;
+  ld8 = (cols + 15) & ~15u;
+  size_t plan = 0;
+  plan += tiles * (size_t)kTileBytes + (tiles + 1) * 4;
+  plan += (quant == AES_QUANT_UNSIGNED_ROW) ? rows * 4ull : 0;
+  plan += (rows + 1) * 4ull + nnz * 6ull;
+  plan += (n_sample_tiles + 2ull * split + 2) * 4;
+  plan += (size_t)maxB * (ld32 * 4ull + ld8 + (size_t)n_sample_rows * 4 + split * 8ull +
+                          (size_t)split * cap * 8 + nslots * 8ull + 4 + p.k_max * 8ull);
+  plan += rows * 4ull;  // slow-path key array
+  if (p.mem_limit && plan > p.mem_limit)
+    return fail(AES_ERR_NOMEM, "matrix needs " + std::to_string(plan) +
+                                   " device bytes, over the handle limit " +
+                                   std::to_string(p.mem_limit));
+  size_t freeb = 0, totalb = 0;
+  AES_CK(cudaMemGetInfo(&freeb, &totalb));
+  if (plan + (64ull << 20) > freeb)
+    return fail(AES_ERR_NOMEM, "matrix needs " + std::to_string(plan) + " device bytes, " +
+                                   std::to_string(freeb) + " free");
+
+  int rc2 = 0;
+#define AES_AL(ptr, n) if ((rc2 = dalloc(&(ptr), (n))) != AES_OK) return rc2
+  AES_AL(d_tiles, tiles * 128);
+  AES_AL(d_tile_rowbase, tiles + 1);
+  if (quant == AES_QUANT_UNSIGNED_ROW) AES_AL(d_rowscale, rows);
+  AES_AL(d_csr_ptr, rows + 1);
+  AES_AL(d_csr_col, std::max<uint64_t>(nnz, 1));
+  AES_AL(d_csr_val, std::max<uint64_t>(nnz, 1));
+  AES_AL(d_sample_first, std::max<uint32_t>(n_sample_tiles, 1));
+  AES_AL(d_part_sample_begin, split + 1);
+  AES_AL(d_part_r, split);
+  AES_AL(d_q32, (size_t)maxB * ld32);
+  AES_AL(d_q8, (size_t)maxB * ld8);
+  AES_AL(d_sample_keys, (size_t)maxB * std::max<uint32_t>(n_sample_rows, 1));
+  AES_AL(d_thr, (size_t)maxB * split);
+  AES_AL(d_cnt, (size_t)maxB * split);
+  AES_AL(d_surv, (size_t)maxB * split * cap);
+  AES_AL(d_cand, (size_t)maxB * std::max<uint32_t>(nslots, 1));
+  AES_AL(d_cand_key, (size_t)maxB * std::max<uint32_t>(nslots, 1));
+  AES_AL(d_status, maxB);
+  AES_AL(d_out_idx, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_allkeys, rows);
+#undef AES_AL
+  AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
+  AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
+
+  // ---- upload -----------------------------------------------------------------------------------
+  std::vector<uint32_t> ptr32(rows + 1);
+  std::vector<uint16_t> col16(nnz);
+  for (uint32_t r = 0; r <= rows; r++) ptr32[r] = (uint32_t)m.ptr[r];
+  parallel_for(nnz, 1 << 20, [&](uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; i++) col16[i] = (uint16_t)m.col[i];
+  });
+  AES_CK(cudaMemcpy(d_tiles, pm.tile_bytes.data(), pm.tile_bytes.size(), cudaMemcpyHostToDevice));
+  AES_CK(cudaMemcpy(d_tile_rowbase, pm.tile_rowbase.data(), (tiles + 1) * 4, cudaMemcpyHostToDevice));
+  if (d_rowscale) AES_CK(cudaMemcpy(d_rowscale, pm.rowscale.data(), rows * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemcpy(d_csr_ptr, ptr32.data(), (rows + 1) * 4ull, cudaMemcpyHostToDevice));
+  if (nnz) {
+    AES_CK(cudaMemcpy(d_csr_col, col16.data(), nnz * 2, cudaMemcpyHostToDevice));
+    AES_CK(cudaMemcpy(d_csr_val, m.val.data(), nnz * 4, cudaMemcpyHostToDevice));
+  }
+  if (n_sample_tiles)
+    AES_CK(cudaMemcpy(d_sample_first, sample_first.data(), n_sample_tiles * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemcpy(d_part_sample_begin, part_begin.data(), (split + 1) * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemcpy(d_part_r, part_r.data(), split * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemset(d_q32, 0, (size_t)maxB * ld32 * 4));
+
+  // ---- launch geometry ---------------------------------------------------------------------
+  plain_smem = (size_t)cols * 128 + (size_t)kWarpsPlain * (P - 1) * 32 * 4;
+  for (int mode = 0; mode < 3; mode++) {
+    PlainKernel kf = pick_plain((int)bits, sgn, mode);
+    AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)plain_smem));
+  }
+  int occ = 0;
+  AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), kThreadsPlain, plain_smem));
+  plain_grid = std::max(1, occ) * sm_count;
+  final_smem = ((cols * 4 + 15) & ~15u) + (size_t)npow2 * 8;
+  AES_CK(cudaFuncSetAttribute((const void*)k_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)final_smem));
+  AES_CK(cudaDeviceSynchronize());
+  return AES_OK;
+}
+
+int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
+  PlainArgs a{};
+  a.tiles = d_tiles;
+  a.tile_rowbase = d_tile_rowbase;
+  a.n_tiles = (uint32_t)tiles;
+  a.n_rows = rows;
+  a.cols = cols;
+  a.q8 = d_q8 + (size_t)q * ld8;
+  a.rowscale = d_rowscale;
+  a.split = split;
+  a.slice = slice;
+  a.thr = d_thr + (size_t)q * split;
+  a.cnt = d_cnt + (size_t)q * split;
+  a.surv = d_surv + (size_t)q * split * cap;
+  a.cap = cap;
+  a.sample_first = d_sample_first;
+  a.sample_stride = ss;
+  a.n_sample_tiles = n_sample_tiles;
+  if (mode == MODE_SAMPLE) a.keys_out = d_sample_keys + (size_t)q * n_sample_rows;
+  else if (mode == MODE_ALL) a.keys_out = d_allkeys;
+  int grid = plain_grid;
+  if (mode == MODE_SAMPLE) grid = std::min<int>(grid, (int)((n_sample_tiles + kWarpsPlain - 1) / kWarpsPlain));
+  grid = std::max(grid, 1);
+  pick_plain((int)bits, sgn, mode)<<<grid, kThreadsPlain, plain_smem, s>>>(a);
+  AES_CK(cudaGetLastError());
+  return AES_OK;
+}
+
+int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
+                    cudaStream_t s) {
+  AES_CK(cudaMemsetAsync(d_status, 0, nq * 4ull, s));
+  k_quantize<<<nq, 256, 0, s>>>(d_q, cols, ld32, (int)bits, (int)quant,
+                                (int)prm.query_quant, d_q8, ld8, d_status);
+  AES_CK(cudaGetLastError());
+  for (uint32_t q = 0; q < nq; q++) {
+    int rc = run_plain(MODE_SAMPLE, q, s);
+    if (rc) return rc;
+  }
+  k_threshold<<<dim3(split, nq), 512, 0, s>>>(d_sample_keys, n_sample_rows, d_part_sample_begin,
+                                              split, d_part_r, d_thr, d_cnt);
+  AES_CK(cudaGetLastError());
+  for (uint32_t q = 0; q < nq; q++) {
+    int rc = run_plain(MODE_FILTER, q, s);
+    if (rc) return rc;
+  }
+  SelectArgs sa{};
+  sa.surv = d_surv;
+  sa.cnt = d_cnt;
+  sa.cap = cap;
+  sa.split = split;
+  sa.slice = slice;
+  sa.n_rows = rows;
+  sa.ntop = ntop;
+  sa.cand = d_cand;
+  sa.cand_key = d_cand_key;
+  sa.status = d_status;
+  k_select<false><<<dim3(split, nq), 512, 0, s>>>(sa);
+  AES_CK(cudaGetLastError());
+  FinalArgs fa{};
+  fa.csr_ptr = d_csr_ptr;
+  fa.csr_col = d_csr_col;
+  fa.csr_val = d_csr_val;
+  fa.q32 = d_q;
+  fa.ld32 = ld32;
+  fa.cols = cols;
+  fa.cand = d_cand;
+  fa.nslots = nslots;
+  fa.npow2 = npow2;
+  fa.k = k;
+  fa.out_idx = d_idx;
+  fa.out_score = d_score;
+  fa.status = d_status;
+  k_final<<<nq, 1024, final_smem, s>>>(fa);
+  AES_CK(cudaGetLastError());
+  return AES_OK;
+}
+
+// Exact slow path for the queries whose status reports a threshold miss or an overflow: score
+// every row, select each partition's Top-CK from the full key array, rescore.
+int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
+                   uint32_t* repaired) {
+  AES_CK(cudaMemcpyAsync(h_status, d_status, nq * 4ull, cudaMemcpyDeviceToHost, s));
+  AES_CK(cudaStreamSynchronize(s));
+  uint32_t nrep = 0;
+  for (uint32_t q = 0; q < nq; q++) {
+    if (h_status[q] & ST_QUERY) return fail(AES_ERR_QUERY, "query " + std::to_string(q) +
+                                               " has negative entries under an unsigned quantiser");
+  }
+  for (uint32_t q = 0; q < nq; q++) {
+    if (!(h_status[q] & (ST_OVERFLOW | ST_MISS))) continue;
+    nrep++;
+    int rc = run_plain(MODE_ALL, q, s);
+    if (rc) return rc;
+    SelectArgs sa{};
+    sa.allkeys = d_allkeys;
+    sa.q0 = q;
+    sa.split = split;
+    sa.slice = slice;
+    sa.n_rows = rows;
+    sa.ntop = ntop;
+    sa.cand = d_cand;
+    sa.cand_key = d_cand_key;
+    sa.status = d_status;
+    k_select<true><<<dim3(split, 1), 512, 0, s>>>(sa);
+    AES_CK(cudaGetLastError());
+    FinalArgs fa{};
+    fa.csr_ptr = d_csr_ptr;
+    fa.csr_col = d_csr_col;
+    fa.csr_val = d_csr_val;
+    fa.q32 = last_q32 + (size_t)q * ld32;
+    fa.ld32 = ld32;
+    fa.cols = cols;
+    fa.cand = d_cand + (size_t)q * nslots;
+    fa.nslots = nslots;
+    fa.npow2 = npow2;
+    fa.k = k;
+    fa.out_idx = d_idx + (size_t)q * k;
+    fa.out_score = d_score + (size_t)q * k;
+    fa.status = nullptr;
+    k_final<<<1, 1024, final_smem, s>>>(fa);
+    AES_CK(cudaGetLastError());
+  }
+  if (nrep) {
+    AES_CK(cudaMemsetAsync(d_status, 0, nq * 4ull, s));
+    AES_CK(cudaStreamSynchronize(s));
+  }
+  if (repaired) *repaired = nrep;
+  return AES_OK;
+}
+
+}  // namespace aes
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+using aes::Engine;
+
+struct aes_handle {
+  Engine e;
+};
+
+extern "C" {
+
+void aes_params_default(aes_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->bits = 6;           // QUANTIZE_B, types.hpp:148
+  p->quant = AES_QUANT_SYM_GLOBAL;
+  p->query_quant = AES_QQ_NUMPY;
+  p->split = 32;         // SPMV_PARTITIONS, types.hpp:39; SPLIT_NUM, search_best_resparse_ratio.py:26
+  p->ck = 512;           // APPROXIMATE_K, types.hpp:149
+  p->k_max = 100;        // DEFAULT_TOP_K, options.hpp:50
+  p->max_batch = 1;
+  p->pack_parts = 32;
+  p->device = 0;
+}
+
+const char* aes_last_error(void) { return aes::last_error_cstr(); }
+
+static int validate_params(const aes_params* p, uint32_t rows, uint32_t cols) {
+  using aes::fail;
+  if (!p) return fail(AES_ERR_INVALID, "params is NULL");
+  if (p->bits != 4 && p->bits != 6 && p->bits != 8)
+    return fail(AES_ERR_UNSUPPORTED, "bits must be 4, 6 or 8");
+  if (p->quant > AES_QUANT_UNSIGNED_GLOBAL) return fail(AES_ERR_INVALID, "unknown quantiser");
+  if (p->query_quant > AES_QQ_TRUNC) return fail(AES_ERR_INVALID, "unknown query quantiser");
+  if (p->query_quant == AES_QQ_TRUNC && p->quant != AES_QUANT_SYM_GLOBAL)
+    return fail(AES_ERR_INVALID, "the truncating query quantiser is signed");
+  if (rows == 0) return fail(AES_ERR_INVALID, "rows must be > 0");
+  if (cols == 0 || cols > aes::kMaxCols)
+    return fail(AES_ERR_UNSUPPORTED, "cols must be in [1, 1024] (10-bit column field)");
+  uint32_t S = p->split <= 1 ? 1 : p->split;
+  if (p->ck < S) return fail(AES_ERR_INVALID, "ck must be >= split");
+  if (p->ck / S * S > 4096) return fail(AES_ERR_UNSUPPORTED, "ck above 4096");
+  if (p->k_max == 0 || p->k_max > 1024) return fail(AES_ERR_UNSUPPORTED, "k_max must be in [1, 1024]");
+  if (p->max_batch == 0 || p->max_batch > 65535) return fail(AES_ERR_INVALID, "max_batch out of range");
+  return AES_OK;
+}
+
+static int create_common(aes::HostCSR& m, const aes_params* p, aes_handle** out) {
+  aes_handle* h = new (std::nothrow) aes_handle();
+  if (!h) return aes::fail(AES_ERR_NOMEM, "host allocation failed");
+  int rc = h->e.build(m, *p);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return AES_OK;
+}
+
+int aes_create(const uint32_t* row, const uint32_t* col, const float* val, uint32_t rows,
+               uint32_t cols, uint64_t nnz, const aes_params* p, aes_handle** out) {
+  if (!out) return aes::fail(AES_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate_params(p, rows, cols);
+  if (rc) return rc;
+  if (nnz && (!row || !col || !val)) return aes::fail(AES_ERR_INVALID, "NULL COO array");
+  aes::HostCSR m;
+  rc = aes::coo_to_csr(row, col, val, rows, cols, nnz, &m);
+  if (rc) return rc;
+  return create_common(m, p, out);
+}
+
+int aes_create_csr(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                   uint32_t cols, const aes_params* p, aes_handle** out) {
+  if (!out) return aes::fail(AES_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate_params(p, rows, cols);
+  if (rc) return rc;
+  if (!ptr) return aes::fail(AES_ERR_INVALID, "NULL CSR array");
+  if (ptr[rows] && (!col || !val)) return aes::fail(AES_ERR_INVALID, "NULL CSR array");
+  rc = aes::check_csr(ptr, col, rows, cols);
+  if (rc) return rc;
+  aes::HostCSR m;
+  m.rows = rows;
+  m.cols = cols;
+  m.ptr.assign(ptr, ptr + rows + 1);
+  m.col.assign(col, col + ptr[rows]);
+  m.val.assign(val, val + ptr[rows]);
+  return create_common(m, p, out);
+}
+
+int aes_pack_host(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                  uint32_t cols, const aes_params* p, uint8_t* packets, uint64_t cap_packets,
+                  uint64_t* n_packets, uint32_t* tile_rowbase) {
+  if (!n_packets || !ptr) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  int rc = validate_params(p, rows, cols);
+  if (rc) return rc;
+  rc = aes::check_csr(ptr, col, rows, cols);
+  if (rc) return rc;
+  aes::HostCSR m;
+  m.rows = rows;
+  m.cols = cols;
+  m.ptr.assign(ptr, ptr + rows + 1);
+  m.col.assign(col, col + ptr[rows]);
+  m.val.assign(val, val + ptr[rows]);
+  aes::PackedMatrix pm;
+  rc = aes::quantize_and_pack(m, *p, &pm);
+  if (rc) return rc;
+  *n_packets = pm.packets;
+  if (packets) {
+    if (cap_packets < pm.packets) return aes::fail(AES_ERR_INVALID, "packet buffer too small");
+    std::vector<uint8_t> flat;
+    aes::untile_packets(pm, &flat);
+    std::memcpy(packets, flat.data(), flat.size());
+  }
+  if (tile_rowbase) std::memcpy(tile_rowbase, pm.tile_rowbase.data(), pm.tile_rowbase.size() * 4);
+  return AES_OK;
+}
+
+int aes_destroy(aes_handle* h) {
+  if (!h) return AES_OK;
+  delete h;
+  return AES_OK;
+}
+
+int aes_get_info(const aes_handle* h, aes_info* info) {
+  if (!h || !info) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  const Engine& e = h->e;
+  std::memset(info, 0, sizeof(*info));
+  info->rows = e.rows;
+  info->cols = e.cols;
+  info->bits = e.bits;
+  info->packet_elems = e.P;
+  info->nnz = e.nnz;
+  info->quantized_nnz = e.qnnz;
+  info->packets = e.packets;
+  info->tiles = e.tiles;
+  info->packet_bytes = e.packets * 64ull;
+  info->device_bytes = e.bytes;
+  info->split = e.split;
+  info->ck = e.nslots;
+  info->ck_effective = e.ck_eff;
+  info->sample_tiles = e.n_sample_tiles;
+  info->sample_rows = e.n_sample_rows;
+  info->max_batch = e.maxB;
+  info->batch_tile = 1;
+  return AES_OK;
+}
+
+int aes_set_query(aes_handle* h, const float* q, uint32_t nq) {
+  if (!h || !q) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  if (nq == 0 || nq > e.maxB) return aes::fail(AES_ERR_INVALID, "nq must be in [1, max_batch]");
+  cudaSetDevice(e.device);
+  for (uint32_t i = 0; i < nq; i++) std::memcpy(e.h_q32 + (size_t)i * e.ld32, q + (size_t)i * e.cols, e.cols * 4ull);
+  AES_CK(cudaMemcpyAsync(e.d_q32, e.h_q32, (size_t)nq * e.ld32 * 4, cudaMemcpyHostToDevice, e.stream));
+  e.nq_loaded = nq;
+  return AES_OK;
+}
+
+int aes_run(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint64_t* ns) {
+  if (!h || !out_idx || !out_score) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  if (!e.nq_loaded) return aes::fail(AES_ERR_STATE, "aes_set_query must come first");
+  if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
+  cudaSetDevice(e.device);
+  const uint32_t nq = e.nq_loaded;
+  e.last_q32 = e.d_q32;
+  AES_CK(cudaEventRecord(e.ev0, e.stream));
+  int rc = e.enqueue(e.d_q32, nq, k, e.d_out_idx, e.d_out_score, e.stream);
+  if (rc) return rc;
+  AES_CK(cudaEventRecord(e.ev1, e.stream));
+  uint32_t rep = 0;
+  rc = e.repair(nq, k, e.d_out_idx, e.d_out_score, e.stream, &rep);
+  if (rc) return rc;
+  AES_CK(cudaMemcpyAsync(out_idx, e.d_out_idx, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, e.stream));
+  AES_CK(cudaMemcpyAsync(out_score, e.d_out_score, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, e.stream));
+  AES_CK(cudaStreamSynchronize(e.stream));
+  if (ns) {
+    float ms = 0.0f;
+    AES_CK(cudaEventElapsedTime(&ms, e.ev0, e.ev1));
+    *ns = (uint64_t)((double)ms * 1e6);
+  }
+  e.last_nq = nq;
+  e.last_k = k;
+  e.ran = true;
+  return AES_OK;
+}
+
+int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t k,
+                   uint32_t* d_idx, float* d_score, void* stream) {
+  if (!h || !d_queries || !d_idx || !d_score) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  if (nq == 0 || nq > e.maxB) return aes::fail(AES_ERR_INVALID, "nq must be in [1, max_batch]");
+  if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
+  cudaSetDevice(e.device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : e.stream;
+  if (e.ld32 != e.cols) {
+    // the device kernels read queries with the padded stride; stage through the handle buffer
+    AES_CK(cudaMemcpy2DAsync(e.d_q32, e.ld32 * 4ull, d_queries, e.cols * 4ull, e.cols * 4ull, nq,
+                             cudaMemcpyDeviceToDevice, s));
+    d_queries = e.d_q32;
+  }
+  e.last_q32 = d_queries;
+  int rc = e.enqueue(d_queries, nq, k, d_idx, d_score, s);
+  if (rc) return rc;
+  e.last_nq = nq;
+  e.last_k = k;
+  e.last_idx = d_idx;
+  e.last_score = d_score;
+  e.last_stream = s;
+  e.last_from_device = true;
+  e.ran = true;
+  return AES_OK;
+}
+
+int aes_finish(aes_handle* h, uint32_t* repaired) {
+  if (!h) return aes::fail(AES_ERR_INVALID, "NULL handle");
+  Engine& e = h->e;
+  if (repaired) *repaired = 0;
+  if (!e.last_from_device) return AES_OK;
+  cudaSetDevice(e.device);
+  int rc = e.repair(e.last_nq, e.last_k, e.last_idx, e.last_score, e.last_stream, repaired);
+  e.last_from_device = false;
+  return rc;
+}
+
+int aes_score_all(aes_handle* h, const float* q, uint32_t* keys) {
+  if (!h || !q || !keys) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  cudaSetDevice(e.device);
+  std::memcpy(e.h_q32, q, e.cols * 4ull);
+  AES_CK(cudaMemcpyAsync(e.d_q32, e.h_q32, e.ld32 * 4ull, cudaMemcpyHostToDevice, e.stream));
+  AES_CK(cudaMemsetAsync(e.d_status, 0, 4, e.stream));
+  aes::dev::k_quantize<<<1, 256, 0, e.stream>>>(e.d_q32, e.cols, e.ld32, (int)e.bits, (int)e.quant,
+                                                (int)e.prm.query_quant, e.d_q8, e.ld8, e.d_status);
+  AES_CK(cudaGetLastError());
+  int rc = e.run_plain(aes::dev::MODE_ALL, 0, e.stream);
+  if (rc) return rc;
+  uint32_t st = 0;
+  AES_CK(cudaMemcpyAsync(keys, e.d_allkeys, e.rows * 4ull, cudaMemcpyDeviceToHost, e.stream));
+  AES_CK(cudaMemcpyAsync(&st, e.d_status, 4, cudaMemcpyDeviceToHost, e.stream));
+  AES_CK(cudaStreamSynchronize(e.stream));
+  e.nq_loaded = 0;
+  if (st & aes::dev::ST_QUERY) return aes::fail(AES_ERR_QUERY, "query has negative entries under an unsigned quantiser");
+  return AES_OK;
+}
+
+int aes_read_candidates(aes_handle* h, uint32_t query, uint32_t* idx, int32_t* score_i32,
+                        float* key_f32, uint32_t cap, uint32_t* n) {
+  if (!h || !n) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  if (!e.ran) return aes::fail(AES_ERR_STATE, "no run yet");
+  if (query >= e.last_nq) return aes::fail(AES_ERR_INVALID, "query index out of range");
+  cudaSetDevice(e.device);
+  std::vector<uint32_t> rows(e.nslots), keys(e.nslots);
+  AES_CK(cudaMemcpy(rows.data(), e.d_cand + (size_t)query * e.nslots, e.nslots * 4ull, cudaMemcpyDeviceToHost));
+  AES_CK(cudaMemcpy(keys.data(), e.d_cand_key + (size_t)query * e.nslots, e.nslots * 4ull, cudaMemcpyDeviceToHost));
+  std::vector<std::pair<uint32_t, uint32_t>> c;
+  for (uint32_t i = 0; i < e.nslots; i++)
+    if (rows[i] != 0xFFFFFFFFu) c.emplace_back(keys[i], rows[i]);
+  std::sort(c.begin(), c.end(), [](const std::pair<uint32_t, uint32_t>& a,
+                                   const std::pair<uint32_t, uint32_t>& b) {
+    return a.first != b.first ? a.first > b.first : a.second > b.second;
+  });
+  uint32_t m = (uint32_t)std::min<size_t>(c.size(), cap);
+  for (uint32_t i = 0; i < m; i++) {
+    if (idx) idx[i] = c[i].second;
+    uint32_t kk = c[i].first;
+    bool fkey = (e.quant == AES_QUANT_UNSIGNED_ROW);
+    float kf;
+    if (fkey) {
+      uint32_t u = (kk & 0x80000000u) ? (kk & 0x7FFFFFFFu) : ~kk;
+      std::memcpy(&kf, &u, 4);
+    } else {
+      kf = (float)(int32_t)(kk ^ 0x80000000u);
+    }
+    if (key_f32) key_f32[i] = kf;
+    if (score_i32) score_i32[i] = fkey ? 0 : (int32_t)(kk ^ 0x80000000u);
+  }
+  *n = (uint32_t)c.size();
+  return AES_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,726 @@
+// aes_kernels.cuh -- sm_103a kernels of the two-stage low-bit Top-K SpMV engine.
+//
+// Stages (reference: zhaijiaqi/AccelES):
+//   k_quantize        quantify_vector (quantify_util.py:31-49) / quantize_vec
+//                     (quantize_utils.hpp:8-18), float64 arithmetic, one CTA per query
+//   k_cand_plain      the low-bit candidate pass of spmv_ucsr_top_k_main
+//                     (spmv_ucsr_top_k_multicore.hpp:195-413; CPU gold spmv_coo_gold_top_k_2,
+//                     gold_algorithms.hpp:249-308): streams Ultra-CSR tiles, decodes flags,
+//                     10-bit columns and B-bit values in registers, integer row scores
+//   k_threshold       per (query, partition) lower bound of the Top-CK boundary from a sample
+//   k_select          exact Top-CK per partition, (key desc, row desc)
+//                     (split_approximate, quantify_util.py:173-196; sort_tuples order)
+//   k_final           FP32 rescoring of the candidates (quantify_util.py:354-356 in FP32;
+//                     gold_algorithms.hpp:211-239 summation order) and the final Top-K
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace aes {
+namespace dev {
+
+constexpr int kWarpsPlain = 16;      // warps per CTA of the plain candidate pass
+constexpr int kThreadsPlain = kWarpsPlain * 32;
+
+enum Mode : int { MODE_FILTER = 0, MODE_SAMPLE = 1, MODE_ALL = 2 };
+
+// status bits per query
+constexpr uint32_t ST_OVERFLOW = 1u;  // survivors exceeded the buffer
+constexpr uint32_t ST_MISS = 2u;      // fewer survivors than candidates needed
+constexpr uint32_t ST_QUERY = 4u;     // query rejected by the quantiser
+
+__host__ __device__ constexpr int packet_elems(int B) { return 511 / (B + 11); }
+
+// order-preserving keys
+__device__ __forceinline__ uint32_t key_i32(int32_t s) { return (uint32_t)s ^ 0x80000000u; }
+__device__ __forceinline__ uint32_t key_f32(float f) {
+  if (f == 0.0f) f = 0.0f;  // -0 == +0 in sort_tuples
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_to_f32(uint32_t k) {
+  uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+  return __uint_as_float(u);
+}
+
+// compile-time field extraction from the 16 words of a 512-bit packet
+template <int POS, int W>
+__device__ __forceinline__ uint32_t ufield(const uint32_t (&w)[16]) {
+  constexpr int k = POS >> 5, s = POS & 31;
+  constexpr uint32_t mask = (W == 32) ? 0xFFFFFFFFu : ((1u << W) - 1u);
+  if constexpr (s + W <= 32) {
+    return (w[k] >> s) & mask;
+  } else {
+    return __funnelshift_r(w[k], w[k + 1], s) & mask;
+  }
+}
+template <int POS, int W>
+__device__ __forceinline__ int32_t sfield(const uint32_t (&w)[16]) {
+  constexpr int k = POS >> 5, s = POS & 31;
+  if constexpr (s + W <= 32) {
+    return (int32_t)(w[k] << (32 - s - W)) >> (32 - W);
+  } else {
+    uint32_t x = __funnelshift_r(w[k], w[k + 1], s);
+    return (int32_t)(x << (32 - W)) >> (32 - W);
+  }
+}
+
+struct PlainArgs {
+  const uint4* tiles;           // n_tiles * 128 uint4 (tiled layout, see aes_host.hpp)
+  const uint32_t* tile_rowbase; // n_tiles + 1
+  uint32_t n_tiles, n_rows, cols;
+  const int8_t* q8;             // quantised query [cols]
+  const float* rowscale;        // per-row scale (unsigned per-row mode) or nullptr
+  uint32_t split, slice;        // row partition of a row: min(row / slice, split - 1)
+  const uint32_t* thr;          // [split] (MODE_FILTER)
+  uint32_t* cnt;                // [split]
+  uint2* surv;                  // [split][cap] (key, row)
+  uint32_t cap;
+  uint32_t* keys_out;           // MODE_SAMPLE: [sample rows]; MODE_ALL: [n_rows]
+  const uint32_t* sample_first; // MODE_SAMPLE: owned-row offset per sample tile
+  uint32_t sample_stride, n_sample_tiles;
+};
+
+__device__ __forceinline__ uint32_t part_of(uint32_t row, uint32_t split, uint32_t slice) {
+  if (split <= 1) return 0;
+  uint32_t p = slice ? row / slice : split - 1;
+  return p < split - 1 ? p : split - 1;
+}
+
+template <int MODE>
+__device__ __forceinline__ void emit_row(const PlainArgs& a, uint32_t row, int32_t score,
+                                         uint32_t sample_tile) {
+  uint32_t key;
+  if (a.rowscale) key = key_f32(__fmul_rn(__int2float_rn(score), __ldg(a.rowscale + row)));
+  else key = key_i32(score);
+  if constexpr (MODE == MODE_FILTER) {
+    uint32_t p = part_of(row, a.split, a.slice);
+    if (key >= __ldg(a.thr + p)) {
+      uint32_t i = atomicAdd(a.cnt + p, 1u);
+      if (i < a.cap) a.surv[(size_t)p * a.cap + i] = make_uint2(key, row);
+    }
+  } else if constexpr (MODE == MODE_SAMPLE) {
+    a.keys_out[row - __ldg(a.sample_first + sample_tile)] = key;
+  } else {
+    a.keys_out[row] = key;
+  }
+}
+
+__device__ __forceinline__ void load_tile(const uint4* tiles, uint32_t t, uint32_t lane,
+                                          uint32_t (&w)[16]) {
+  const uint4* base = tiles + (size_t)t * 128 + lane;
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    uint4 v = __ldcs(base + s * 32);
+    w[4 * s + 0] = v.x;
+    w[4 * s + 1] = v.y;
+    w[4 * s + 2] = v.z;
+    w[4 * s + 3] = v.w;
+  }
+}
+
+// Per-lane decode of one packet: prefix sums S_j of val_j * q[col_j] (int32, wrapping), S_j
+// for j < P-1 staged in E[j][lane]; returns the packet total S_{P-1}.
+template <int B, bool SGN>
+struct PacketDecoder {
+  static constexpr int P = packet_elems(B);
+  template <int J>
+  __device__ __forceinline__ static void step(const uint32_t (&w)[16], const int32_t* qt,
+                                              uint32_t lane, uint32_t* E, int32_t& S) {
+    if constexpr (J < P) {
+      const uint32_t col = ufield<P + 10 * J, 10>(w);
+      int32_t v;
+      if constexpr (SGN) v = sfield<11 * P + B * J, B>(w);
+      else v = (int32_t)ufield<11 * P + B * J, B>(w);
+      const int32_t q = qt[(col << 5) | lane];
+      S += v * q;
+      if constexpr (J < P - 1) E[J * 32 + lane] = (uint32_t)S;
+      step<J + 1>(w, qt, lane, E, S);
+    }
+  }
+  __device__ __forceinline__ static int32_t run(const uint32_t (&w)[16], const int32_t* qt,
+                                                uint32_t lane, uint32_t* E) {
+    int32_t S = 0;
+    step<0>(w, qt, lane, E, S);
+    return S;
+  }
+  __device__ __forceinline__ static uint64_t flags(const uint32_t (&w)[16]) {
+    if constexpr (P <= 32) {
+      return (uint64_t)(w[0] & ((P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u)));
+    } else {
+      return (uint64_t)w[0] | ((uint64_t)(w[1] & ((1u << (P - 32)) - 1u)) << 32);
+    }
+  }
+};
+
+__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, uint32_t lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t u = __shfl_up_sync(0xFFFFFFFFu, v, d);
+    if (lane >= (uint32_t)d) v += u;
+  }
+  return v;
+}
+
+// One warp streams tiles [tb, te) and owns every row whose first entry lies in them; the row
+// still open at te is finished by reading on until the next row flag.
+template <int B, bool SGN, int MODE>
+__device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te, uint32_t sample_tile,
+                           const int32_t* qt, uint32_t* E) {
+  using D = PacketDecoder<B, SGN>;
+  constexpr int P = D::P;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (tb >= te) return;
+  bool open_owned = (tb == 0);  // row 0 starts at entry 0 without a flag
+  uint32_t startG = 0;          // running sum before the open row's first entry
+  uint32_t carryG = 0;          // running sum before the current tile
+  uint32_t w[16], nw[16];
+  load_tile(a.tiles, tb, lane, w);
+  for (uint32_t t = tb;; t++) {
+    if (t >= a.n_tiles) {  // end of the matrix closes the last row
+      if (open_owned && lane == 0) emit_row<MODE>(a, a.n_rows - 1, (int32_t)(carryG - startG), sample_tile);
+      return;
+    }
+    const bool closing = (t >= te);
+    if (t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
+    const uint64_t F = D::flags(w);
+    const int32_t total = D::run(w, qt, lane, E);
+    __syncwarp();
+    const uint32_t incl = warp_incl_sum((uint32_t)total, lane);
+    const uint32_t LB = carryG + incl - (uint32_t)total;  // running sum before this packet
+    const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
+    if (closing) {
+      if (has_mask == 0) {  // the open row spans this whole tile
+        carryG += tileSum;
+#pragma unroll
+        for (int i = 0; i < 16; i++) w[i] = nw[i];
+        continue;
+      }
+      const uint32_t l0 = __ffs(has_mask) - 1;
+      if (lane == l0) {
+        const int j0 = __ffsll((long long)F) - 1;
+        const uint32_t Gb = LB + (j0 ? E[(j0 - 1) * 32 + lane] : 0u);
+        if (open_owned) {
+          const uint32_t fl = __ldg(a.tile_rowbase + t) + 0u;
+          // rows completed before lane l0 in this tile: none (l0 is the first lane with a flag)
+          emit_row<MODE>(a, fl, (int32_t)(Gb - startG), sample_tile);
+        }
+      }
+      return;
+    }
+    // flags before this lane -> row ids
+    const uint32_t nf = (uint32_t)__popcll(F);
+    const uint32_t nf_incl = warp_incl_sum(nf, lane);
+    const uint32_t rbase = __ldg(a.tile_rowbase + t) + nf_incl - nf;
+    // G before the last flag of each lane, inherited by lanes to its right
+    uint32_t lastGb = 0;
+    if (F) {
+      const int jl = 63 - __clzll((long long)F);
+      lastGb = LB + (jl ? E[(jl - 1) * 32 + lane] : 0u);
+    }
+    const uint32_t left = has_mask & ((1u << lane) - 1u);
+    uint32_t src = left ? (31 - __clz(left)) : 0u;
+    uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, src);
+    uint32_t prevG = left ? inhG : startG;
+    bool owned = left ? true : open_owned;
+    // completed rows: the k-th flag of this lane closes row rbase + k
+    uint64_t f = F;
+    uint32_t k = 0;
+    while (f) {
+      const int j = __ffsll((long long)f) - 1;
+      f &= f - 1;
+      const uint32_t Gb = LB + (j ? E[(j - 1) * 32 + lane] : 0u);
+      if (owned) emit_row<MODE>(a, rbase + k, (int32_t)(Gb - prevG), sample_tile);
+      prevG = Gb;
+      owned = true;
+      k++;
+    }
+    if (has_mask) {
+      const uint32_t lhi = 31 - __clz(has_mask);
+      startG = __shfl_sync(0xFFFFFFFFu, lastGb, lhi);
+      open_owned = true;
+    }
+    carryG += tileSum;
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 16; i++) w[i] = nw[i];
+  }
+}
+
+template <int B, bool SGN, int MODE>
+__global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int P = packet_elems(B);
+  int32_t* qt = reinterpret_cast<int32_t*>(smem);                 // [cols][32]
+  uint32_t* Eall = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * 128);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  uint32_t* E = Eall + warp * (P - 1) * 32;
+  // replicate the query once per lane so that lane l always reads bank l
+  for (uint32_t i = threadIdx.x; i < a.cols * 32u; i += blockDim.x) {
+    const uint32_t c = i >> 5;
+    int32_t v = SGN ? (int32_t)a.q8[c] : (int32_t)(uint8_t)a.q8[c];
+    qt[i] = v;
+  }
+  __syncthreads();
+  const uint32_t gw = blockIdx.x * kWarpsPlain + warp;
+  const uint32_t nw = gridDim.x * kWarpsPlain;
+  if constexpr (MODE == MODE_SAMPLE) {
+    for (uint32_t s = gw; s < a.n_sample_tiles; s += nw) {
+      const uint32_t t = s * a.sample_stride;
+      cand_range<B, SGN, MODE>(a, t, t + 1, s, qt, E);
+    }
+  } else {
+    const uint64_t n = a.n_tiles;
+    const uint32_t tb = (uint32_t)((n * gw) / nw), te = (uint32_t)((n * (gw + 1)) / nw);
+    cand_range<B, SGN, MODE>(a, tb, te, 0, qt, E);
+  }
+  (void)lane;
+}
+
+}  // namespace dev
+}  // namespace aes
+
+namespace aes {
+namespace dev {
+
+// ---------------------------------------------------------------------------------------------
+// query quantiser: one CTA per query, float64 arithmetic as numpy's (IEEE division and
+// multiplication, round half to even), so the integer query is bit-identical to
+// quantify_vector (quantify_util.py:31-49) applied to the float64 upcast of the FP32 query.
+// quant: 0 symmetric, 1/2 unsigned (per query); qq: 0 numpy, 1 quantize_vec truncation.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_t ld32, int bits,
+                           int quant, int qq, int8_t* __restrict__ q8, uint32_t ld8,
+                           uint32_t* __restrict__ status) {
+  __shared__ float red[32];
+  __shared__ int negs;
+  const float* x = q32 + (size_t)blockIdx.x * ld32;
+  int8_t* o = q8 + (size_t)blockIdx.x * ld8;
+  if (qq == 1) {  // quantize_utils.hpp:8-18 (ap_fixed<32,B,AP_TRN_ZERO>, to_int, ap_int<B>)
+    const int F = 32 - bits;
+    for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) {
+      double v = (double)x[j] * ldexp(1.0, bits - 2 + F);
+      long long X = (long long)trunc(v);
+      int32_t X32 = (int32_t)(uint32_t)(unsigned long long)X;
+      int32_t n = X32 / (int32_t)(1u << F);
+      int32_t mask = (1 << bits) - 1, half = 1 << (bits - 1);
+      o[j] = (int8_t)(((n & mask) ^ half) - half);
+    }
+    return;
+  }
+  float m = 0.0f;
+  int neg = 0;
+  for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) {
+    float v = x[j];
+    neg |= (v < 0.0f);
+    m = fmaxf(m, quant == 0 ? fabsf(v) : v);
+  }
+  if (threadIdx.x == 0) negs = 0;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, d));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  if (neg) atomicOr(&negs, 1);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float r = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) r = fmaxf(r, __shfl_xor_sync(0xFFFFFFFFu, r, d));
+    if (threadIdx.x == 0) red[0] = r;
+  }
+  __syncthreads();
+  const double mm = (double)red[0];  // max |x| (or max x) is exact in float64
+  if (quant != 0 && negs) {
+    if (threadIdx.x == 0) atomicOr(status + blockIdx.x, ST_QUERY);
+    for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) o[j] = 0;
+    return;
+  }
+  const int32_t M = quant == 0 ? ((1 << bits) - 1) / 2 : (1 << bits) - 1;
+  const int32_t lo = quant == 0 ? -M - 1 : 0;
+  for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) {
+    int32_t q = 0;
+    if (mm != 0.0) {
+      double y = (double)M * ((double)x[j] / mm);
+      q = (int32_t)rint(y);
+      q = q < lo ? lo : (q > M ? M : q);
+    }
+    o[j] = (int8_t)(uint8_t)(uint32_t)q;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// block helpers
+// ---------------------------------------------------------------------------------------------
+constexpr int kHistBins = 2048;
+
+// Largest bin b with sum(hist[b..]) >= need; *above = sum(hist[b+1..]).  Executed by warp 0.
+__device__ __forceinline__ void warp_find_suffix_bin(const uint32_t* hist, int nbins,
+                                                     uint32_t need, int* bin_out,
+                                                     uint32_t* above_out) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const int per = nbins / 32;
+  // lane l owns bins [l*per, (l+1)*per); suffix sums from the top
+  uint32_t own = 0;
+  for (int i = 0; i < per; i++) own += hist[lane * per + i];
+  // exclusive suffix over lanes: sum of lanes > l
+  uint32_t incl = own;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t u = __shfl_down_sync(0xFFFFFFFFu, incl, d);
+    if (lane + d < 32) incl += u;
+  }
+  uint32_t excl = incl - own;  // bins above this lane's chunk
+  // the chunk holding the boundary: excl < need <= incl
+  bool mine = (excl < need) && (incl >= need);
+  uint32_t msk = __ballot_sync(0xFFFFFFFFu, mine);
+  if (msk == 0) {  // need exceeds the total: take everything
+    if (lane == 0) { *bin_out = 0; *above_out = 0; }
+    return;
+  }
+  uint32_t owner = __ffs(msk) - 1;
+  if (lane == owner) {
+    uint32_t acc = excl;
+    int b = (int)(lane * per + per - 1);
+    for (; b >= (int)(lane * per); b--) {
+      uint32_t h = hist[b];
+      if (acc + h >= need) break;
+      acc += h;
+    }
+    *bin_out = b;
+    *above_out = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// k_threshold: per (query, partition), a lower bound L of the r-th largest sample key (exact
+// within 2^shift2), so that every row at or above the partition's Top-CK boundary has a key
+// >= L with overwhelming probability; a miss is detected later (ST_MISS) and repaired.
+// Also resets the partition's survivor counter.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_threshold(const uint32_t* __restrict__ keys, uint32_t ld_keys,
+                            const uint32_t* __restrict__ part_begin, uint32_t split,
+                            const uint32_t* __restrict__ r_part, uint32_t* __restrict__ thr,
+                            uint32_t* __restrict__ cnt) {
+  __shared__ uint32_t hist[kHistBins];
+  __shared__ uint32_t smin[32], smax[32];
+  __shared__ int s_bin;
+  __shared__ uint32_t s_above;
+  const uint32_t p = blockIdx.x, q = blockIdx.y;
+  const uint32_t* kk = keys + (size_t)q * ld_keys;
+  const uint32_t a = part_begin[p], b = part_begin[p + 1];
+  const uint32_t n = b - a;
+  const uint32_t r = r_part[p];
+  uint32_t* T = thr + (size_t)q * split + p;
+  if (threadIdx.x == 0) cnt[(size_t)q * split + p] = 0;
+  if (n < r || r == 0) {
+    if (threadIdx.x == 0) *T = 0;  // too few samples: keep every row of the partition
+    return;
+  }
+  uint32_t mn = 0xFFFFFFFFu, mx = 0;
+  for (uint32_t i = a + threadIdx.x; i < b; i += blockDim.x) {
+    uint32_t v = kk[i];
+    mn = min(mn, v);
+    mx = max(mx, v);
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, d));
+    mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, d));
+  }
+  if ((threadIdx.x & 31) == 0) { smin[threadIdx.x >> 5] = mn; smax[threadIdx.x >> 5] = mx; }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t nw = (blockDim.x + 31) / 32;
+    mn = threadIdx.x < nw ? smin[threadIdx.x] : 0xFFFFFFFFu;
+    mx = threadIdx.x < nw ? smax[threadIdx.x] : 0u;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, d));
+      mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, d));
+    }
+    if (threadIdx.x == 0) { smin[0] = mn; smax[0] = mx; }
+  }
+  __syncthreads();
+  mn = smin[0];
+  mx = smax[0];
+  const uint32_t span = mx - mn;
+  if (span == 0) {
+    if (threadIdx.x == 0) *T = mn;
+    return;
+  }
+  const int bl = 32 - __clz(span);           // bits of span
+  const int sh1 = bl > 11 ? bl - 11 : 0;
+  for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (uint32_t i = a + threadIdx.x; i < b; i += blockDim.x)
+    atomicAdd(&hist[(kk[i] - mn) >> sh1], 1u);
+  __syncthreads();
+  if (threadIdx.x < 32) warp_find_suffix_bin(hist, kHistBins, r, &s_bin, &s_above);
+  __syncthreads();
+  const uint32_t b1 = (uint32_t)s_bin, above1 = s_above;
+  if (sh1 == 0) {
+    if (threadIdx.x == 0) *T = mn + b1;
+    return;
+  }
+  const int sh2 = sh1 > 11 ? sh1 - 11 : 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (uint32_t i = a + threadIdx.x; i < b; i += blockDim.x) {
+    uint32_t d = kk[i] - mn;
+    if ((d >> sh1) == b1) atomicAdd(&hist[(d >> sh2) & ((1u << (sh1 - sh2)) - 1u)], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) warp_find_suffix_bin(hist, kHistBins, r - above1, &s_bin, &s_above);
+  __syncthreads();
+  if (threadIdx.x == 0) *T = mn + (b1 << sh1) + ((uint32_t)s_bin << sh2);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Block-wide exact select: the `need` largest 64-bit composites (key << 32 | row) of n items.
+// Items come from an accessor; returns through smem the threshold composite tau such that
+// exactly `need` items are >= tau (composites are unique because rows are).
+// ---------------------------------------------------------------------------------------------
+template <class Get>
+__device__ uint64_t block_select_tau(Get get, uint32_t n, uint32_t need, uint32_t* hist256,
+                                     uint64_t* sh64) {
+  // min / max composite
+  uint64_t mn = ~0ull, mx = 0;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    uint64_t c = get(i);
+    mn = c < mn ? c : mn;
+    mx = c > mx ? c : mx;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    uint64_t a = __shfl_xor_sync(0xFFFFFFFFu, mn, d), b = __shfl_xor_sync(0xFFFFFFFFu, mx, d);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { sh64[threadIdx.x >> 5] = mn; sh64[32 + (threadIdx.x >> 5)] = mx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t nw = (blockDim.x + 31) / 32;
+    uint64_t a = ~0ull, b = 0;
+    for (uint32_t w = 0; w < nw; w++) {
+      a = sh64[w] < a ? sh64[w] : a;
+      b = sh64[32 + w] > b ? sh64[32 + w] : b;
+    }
+    sh64[64] = a;
+    sh64[65] = b;
+  }
+  __syncthreads();
+  mn = sh64[64];
+  mx = sh64[65];
+  if (need >= n) return mn;
+  if (mn == mx) return mn;
+  int hi = 63 - __clzll((long long)(mn ^ mx));
+  uint64_t prefix = mx & ~((hi == 63) ? ~0ull : ((2ull << hi) - 1ull));
+  uint64_t fixed = ~((hi == 63) ? ~0ull : ((2ull << hi) - 1ull));
+  uint32_t need_rem = need;
+  while (true) {
+    const int lo = hi >= 7 ? hi - 7 : 0;
+    const int width = hi - lo + 1;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist256[i] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      uint64_t c = get(i);
+      if ((c & fixed) == prefix)
+        atomicAdd(&hist256[(uint32_t)(c >> lo) & ((1u << width) - 1u)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      // 256 bins, 8 per lane
+      const uint32_t lane = threadIdx.x;
+      uint32_t own = 0;
+      for (int i = 0; i < 8; i++) own += hist256[lane * 8 + i];
+      uint32_t incl = own;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t u = __shfl_down_sync(0xFFFFFFFFu, incl, d);
+        if (lane + d < 32) incl += u;
+      }
+      uint32_t excl = incl - own;
+      bool mine = (excl < need_rem) && (incl >= need_rem);
+      uint32_t msk = __ballot_sync(0xFFFFFFFFu, mine);
+      uint32_t owner = msk ? (__ffs(msk) - 1) : 0;
+      if (lane == owner) {
+        uint32_t acc = excl;
+        int bb = lane * 8 + 7;
+        for (; bb > (int)(lane * 8); bb--) {
+          if (acc + hist256[bb] >= need_rem) break;
+          acc += hist256[bb];
+        }
+        sh64[66] = (uint64_t)bb;
+        sh64[67] = (uint64_t)acc;
+        sh64[68] = (uint64_t)hist256[bb];
+      }
+    }
+    __syncthreads();
+    const uint32_t d = (uint32_t)sh64[66];
+    const uint32_t above = (uint32_t)sh64[67];
+    const uint32_t inbin = (uint32_t)sh64[68];
+    __syncthreads();
+    need_rem -= above;
+    prefix |= (uint64_t)d << lo;
+    fixed |= (uint64_t)((1u << width) - 1u) << lo;
+    if (inbin == need_rem || lo == 0) break;
+    hi = lo - 1;
+  }
+  return prefix;
+}
+
+// ---------------------------------------------------------------------------------------------
+// k_select: per (query, partition) exact Top-ntop of the survivors by (key desc, row desc).
+// implicit = true reads every row of the partition from a full key array (slow path).
+// ---------------------------------------------------------------------------------------------
+struct SelectArgs {
+  const uint2* surv;        // [nq][split][cap]
+  const uint32_t* cnt;      // [nq][split]
+  uint32_t cap;
+  const uint32_t* allkeys;  // implicit: [n_rows] keys of query `q0`
+  uint32_t q0;
+  uint32_t split, slice, n_rows, ntop;
+  uint32_t* cand;           // [nq][split*ntop] rows, 0xFFFFFFFF = empty slot
+  uint32_t* cand_key;       // [nq][split*ntop]
+  uint32_t* status;         // [nq]
+};
+
+template <bool IMPLICIT>
+__global__ void k_select(SelectArgs a) {
+  __shared__ uint32_t hist[256];
+  __shared__ uint64_t sh64[72];
+  __shared__ uint32_t s_out;
+  const uint32_t p = blockIdx.x, q = IMPLICIT ? a.q0 : blockIdx.y;
+  const uint32_t r0 = p * a.slice;
+  const uint32_t r1 = (a.split <= 1 || p == a.split - 1) ? a.n_rows : (p + 1) * a.slice;
+  const uint32_t prow = (a.split <= 1) ? a.n_rows : (r1 - r0);
+  const uint32_t need = min(a.ntop, prow);
+  uint32_t* cr = a.cand + ((size_t)q * a.split + p) * a.ntop;
+  uint32_t* ck = a.cand_key + ((size_t)q * a.split + p) * a.ntop;
+  for (uint32_t i = threadIdx.x; i < a.ntop; i += blockDim.x) { cr[i] = 0xFFFFFFFFu; ck[i] = 0; }
+  uint32_t n;
+  if (IMPLICIT) {
+    n = (a.split <= 1) ? a.n_rows : prow;
+  } else {
+    n = a.cnt[(size_t)q * a.split + p];
+    if (n > a.cap) {
+      if (threadIdx.x == 0) atomicOr(a.status + q, ST_OVERFLOW);
+      return;
+    }
+    if (n < need) {
+      if (threadIdx.x == 0) atomicOr(a.status + q, ST_MISS);
+      return;
+    }
+  }
+  const uint32_t base = (a.split <= 1) ? 0 : r0;
+  const uint2* sv = a.surv + ((size_t)q * a.split + p) * a.cap;
+  auto get = [&](uint32_t i) -> uint64_t {
+    if (IMPLICIT) {
+      uint32_t row = base + i;
+      return ((uint64_t)a.allkeys[row] << 32) | row;
+    } else {
+      uint2 v = sv[i];
+      return ((uint64_t)v.x << 32) | v.y;
+    }
+  };
+  __syncthreads();
+  if (need == 0) return;
+  const uint64_t tau = block_select_tau(get, n, need, hist, sh64);
+  if (threadIdx.x == 0) s_out = 0;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    uint64_t c = get(i);
+    if (c >= tau) {
+      uint32_t o = atomicAdd(&s_out, 1u);
+      if (o < a.ntop) {
+        cr[o] = (uint32_t)c;
+        ck[o] = (uint32_t)(c >> 32);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// k_final: FP32 rescoring of every candidate (sequential over the row's entries in column
+// order, separately rounded multiply and add) and the final Top-K in sort_tuples order.
+// One CTA per query; the candidate slots are sorted by a bitonic network in shared memory.
+// ---------------------------------------------------------------------------------------------
+struct FinalArgs {
+  const uint32_t* csr_ptr;   // [rows+1]
+  const uint16_t* csr_col;
+  const float* csr_val;
+  const float* q32;          // [nq][ld32]
+  uint32_t ld32, cols;
+  const uint32_t* cand;      // [nq][nslots]
+  uint32_t nslots, npow2, k;
+  uint32_t* out_idx;         // [nq][k]
+  float* out_score;          // [nq][k]
+  const uint32_t* status;    // [nq]; queries with a set status are left to the repair path
+};
+
+__global__ void __launch_bounds__(1024) k_final(FinalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* qs = reinterpret_cast<float*>(smem);
+  uint64_t* comp = reinterpret_cast<uint64_t*>(smem + ((a.cols * 4 + 15) & ~15u));
+  const uint32_t q = blockIdx.x;
+  if (a.status && a.status[q]) return;
+  const float* x = a.q32 + (size_t)q * a.ld32;
+  for (uint32_t j = threadIdx.x; j < a.cols; j += blockDim.x) qs[j] = x[j];
+  __syncthreads();
+  const uint32_t* cr = a.cand + (size_t)q * a.nslots;
+  for (uint32_t i = threadIdx.x; i < a.npow2; i += blockDim.x) {
+    uint64_t c = 0;
+    if (i < a.nslots) {
+      uint32_t row = cr[i];
+      if (row != 0xFFFFFFFFu) {
+        uint32_t e = a.csr_ptr[row], e1 = a.csr_ptr[row + 1];
+        float acc = 0.0f;
+        for (; e + 4 <= e1; e += 4) {
+          uint16_t c0 = a.csr_col[e], c1 = a.csr_col[e + 1], c2 = a.csr_col[e + 2], c3 = a.csr_col[e + 3];
+          float v0 = a.csr_val[e], v1 = a.csr_val[e + 1], v2 = a.csr_val[e + 2], v3 = a.csr_val[e + 3];
+          acc = __fadd_rn(acc, __fmul_rn(v0, qs[c0]));
+          acc = __fadd_rn(acc, __fmul_rn(v1, qs[c1]));
+          acc = __fadd_rn(acc, __fmul_rn(v2, qs[c2]));
+          acc = __fadd_rn(acc, __fmul_rn(v3, qs[c3]));
+        }
+        for (; e < e1; e++) acc = __fadd_rn(acc, __fmul_rn(a.csr_val[e], qs[a.csr_col[e]]));
+        c = ((uint64_t)key_f32(acc) << 32) | row;
+      }
+    }
+    comp[i] = c;
+  }
+  __syncthreads();
+  // bitonic sort, descending
+  for (uint32_t kk = 2; kk <= a.npow2; kk <<= 1) {
+    for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < a.npow2; i += blockDim.x) {
+        uint32_t l = i ^ j;
+        if (l > i) {
+          uint64_t ci = comp[i], cl = comp[l];
+          bool desc = ((i & kk) == 0);
+          if (desc ? (ci < cl) : (ci > cl)) { comp[i] = cl; comp[l] = ci; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (uint32_t i = threadIdx.x; i < a.k; i += blockDim.x) {
+    uint64_t c = (i < a.npow2) ? comp[i] : 0;
+    uint32_t* oi = a.out_idx + (size_t)q * a.k;
+    float* os = a.out_score + (size_t)q * a.k;
+    if (c == 0) {
+      oi[i] = 0xFFFFFFFFu;
+      os[i] = -__int_as_float(0x7f800000);
+    } else {
+      oi[i] = (uint32_t)c;
+      os[i] = key_to_f32((uint32_t)(c >> 32));
+    }
+  }
+}
+
+}  // namespace dev
+}  // namespace aes

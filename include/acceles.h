@@ -1,0 +1,160 @@
+/*
+ * acceles.h -- C ABI of the GB300 two-stage low-bit Top-K SpMV engine.
+ *
+ * The engine replaces the reference's quantised host driver `struct SpMV`
+ * (zhaijiaqi/AccelES, src/fpga/src/host_spmv_ucsr.cpp:134-829) and its GPU-host twin
+ * (src/gpu/host_spmv_topk_csr_gpu_int8.cu:123-314).  Every entry point takes plain pointers and
+ * sizes, returns a status code (never exits), and is annotated with the reference interface it
+ * stands in for.  One handle owns one device-resident matrix; a handle is used by one host
+ * thread at a time.
+ *
+ * Method (reference README.md:5): the matrix is quantised to B bits and packed as Ultra-CSR
+ * (512-bit packets, types.hpp:151-162); a query is quantised the same way; an integer candidate
+ * pass scores every row and keeps the Top-CK rows per row partition (split); the candidates are
+ * rescored in FP32 against the FP32 matrix and the final Top-K is returned in sort_tuples order
+ * (score descending, row index descending; evaluation_utils.hpp:40-62).
+ */
+#ifndef ACCELES_H
+#define ACCELES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define AES_OK 0
+#define AES_ERR_INVALID (-1)     /* bad argument or malformed matrix */
+#define AES_ERR_UNSUPPORTED (-2) /* bits not in {4,6,8}, cols > 1024, K > 1024, ... */
+#define AES_ERR_CUDA (-3)        /* CUDA runtime failure; aes_last_error() has the text */
+#define AES_ERR_NOMEM (-4)       /* device memory over the handle's limit, or allocation refused */
+#define AES_ERR_QUERY (-5)       /* query rejected (negative entry under an unsigned quantiser) */
+#define AES_ERR_STATE (-6)       /* call out of order (run before set_query, ...) */
+#define AES_ERR_NODEV (-7)       /* no CUDA device */
+
+/* ---- quantiser choices ---------------------------------------------------------------------- */
+/* matrix + query quantiser */
+#define AES_QUANT_SYM_GLOBAL 0      /* quantify_matrix/quantify_vector, symmetric=True
+                                       (quantify_util.py:8-49): the reference's default */
+#define AES_QUANT_UNSIGNED_ROW 1    /* per-row max-scaled unsigned B-bit matrix, per-query
+                                       unsigned query; candidate key = rowscale * int score */
+#define AES_QUANT_UNSIGNED_GLOBAL 2 /* quantify_matrix/quantify_vector, symmetric=False, on
+                                       non-negative data */
+/* query quantiser */
+#define AES_QQ_NUMPY 0 /* quantify_vector (quantify_util.py:31-49) */
+#define AES_QQ_TRUNC 1 /* quantize_vec (quantize_utils.hpp:8-18): trunc(2^(B-2) * v) */
+
+typedef struct aes_handle aes_handle;
+
+typedef struct aes_params {
+  uint32_t bits;          /* B: 4, 6 or 8 (QUANTIZE_B, types.hpp:148) */
+  uint32_t quant;         /* AES_QUANT_* */
+  uint32_t query_quant;   /* AES_QQ_* */
+  uint32_t split;         /* row partitions of the Top-CK select; <= 1 means one global
+                             Top-CK (SPLIT, quantify_util.py:173-196 / SPMV_PARTITIONS) */
+  uint32_t ck;            /* candidates kept (APPROXIMATE_K, types.hpp:149) */
+  uint32_t k_max;         /* largest K a run may request (<= 1024) */
+  uint32_t max_batch;     /* most queries per aes_set_query / aes_run_device call */
+  uint32_t pack_parts;    /* Ultra-CSR packing partitions (SPMV_PARTITIONS = 32) */
+  uint32_t sample_stride; /* threshold sample: one 32-packet tile in this many (0 = auto) */
+  uint32_t batch_tile;    /* queries per matrix pass in the batched kernel (0 = auto) */
+  int32_t device;         /* CUDA device ordinal */
+  uint32_t flags;         /* reserved, 0 */
+  uint64_t seed;          /* seed of the empty-row rule (check_empty_rows is unseeded) */
+  uint64_t mem_limit;     /* device bytes this handle may allocate; 0 = no limit */
+} aes_params;
+
+typedef struct aes_info {
+  uint32_t rows, cols, bits, packet_elems;
+  uint64_t nnz, quantized_nnz, packets, tiles;
+  uint64_t packet_bytes;  /* Ultra-CSR bytes streamed by one full candidate pass */
+  uint64_t device_bytes;  /* device memory held by the handle */
+  uint32_t split, ck, ck_effective, sample_tiles;
+  uint32_t sample_rows, max_batch, batch_tile, reserved;
+} aes_info;
+
+/* Defaults: bits 6, AES_QUANT_SYM_GLOBAL, AES_QQ_NUMPY, split 32, ck 512, k_max 100
+ * (types.hpp:39,148-149; options.hpp:50), max_batch 1, pack_parts 32. */
+void aes_params_default(aes_params* p);
+
+/* Build a device-resident matrix from a COO (any order; duplicates are kept as separate
+ * entries and summed).  Quantises, fixes rows left empty, packs Ultra-CSR and uploads it
+ * together with the FP32 CSR used by the exact pass.  Replaces the quantised constructor
+ * SpMV(ConfigOpenCL&, q_x, q_y, q_val, rows, cols, nnz, q_vec, debug)
+ * (host_spmv_ucsr.cpp:198-218) plus Q_packet_coo (:278) and Q_setup (:501); the caller keeps
+ * ownership of its arrays. */
+int aes_create(const uint32_t* row, const uint32_t* col, const float* val, uint32_t rows,
+               uint32_t cols, uint64_t nnz, const aes_params* p, aes_handle** out);
+/* Same from a CSR already sorted by (row, col): ptr[rows+1]. */
+int aes_create_csr(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                   uint32_t cols, const aes_params* p, aes_handle** out);
+int aes_destroy(aes_handle* h);
+int aes_get_info(const aes_handle* h, aes_info* info);
+
+/* Load nq FP32 queries (row-major [nq][cols], host memory) for the next aes_run.
+ * Replaces Q_reset(q_type* vec, int debug) (host_spmv_ucsr.cpp:790-828) / reset(vec)
+ * (host_spmv_topk_csr_gpu_int8.cu:288); quantisation happens on the device. */
+int aes_set_query(aes_handle* h, const float* q, uint32_t nq);
+
+/* Run the loaded queries: candidate pass, Top-CK select, FP32 rescoring, Top-K.  out_idx and
+ * out_score are host arrays [nq][k]; entries past the number of candidates are row
+ * 0xFFFFFFFF with score -inf.  *ns (may be NULL) receives the device time in nanoseconds.
+ * Replaces operator()(bool, int debug) (host_spmv_ucsr.cpp:556-565) with Q_wait (:605) and the
+ * merge of Q_read_result (:691-748). */
+int aes_run(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint64_t* ns);
+
+/* Candidates of query `query` of the last run in sort_tuples order (key descending, row
+ * descending).  score_i32 gets the integer candidate score, key_f32 the ranking key (the
+ * integer score, or rowscale * score under AES_QUANT_UNSIGNED_ROW); either may be NULL.
+ * Replaces Q_read_result(res, idx, debug) (host_spmv_ucsr.cpp:691-748), which also drops
+ * non-positive FPGA slots; every kept candidate is returned here. */
+int aes_read_candidates(aes_handle* h, uint32_t query, uint32_t* idx, int32_t* score_i32,
+                        float* key_f32, uint32_t cap, uint32_t* n);
+
+/* Device-resident variant: d_queries [nq][cols] FP32 and outputs [nq][k] are device pointers,
+ * `stream` a cudaStream_t (NULL = the handle's stream).  Asynchronous: call aes_finish before
+ * reading the outputs.  No reference counterpart (the reference always stages through host
+ * buffers); it is the resident-input entry a serving loop uses. */
+int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t k,
+                   uint32_t* d_idx, float* d_score, void* stream);
+/* Wait for the last aes_run_device and repair any query whose fast path reported a sample
+ * threshold miss or a survivor-buffer overflow (exact slow path).  *repaired (may be NULL)
+ * receives the number of repaired queries. */
+int aes_finish(aes_handle* h, uint32_t* repaired);
+
+/* Candidate-pass keys of every row for one host FP32 query: keys[rows] receives the
+ * order-preserving key of the integer score (score ^ 0x80000000), or of rowscale * score under
+ * AES_QUANT_UNSIGNED_ROW.  Synchronous.  The integer counterpart of the reference's full SpMV
+ * check (spmv_coo_gold4 + sort_pr in sw_test, host_spmv_ucsr.cpp:841-869). */
+int aes_score_all(aes_handle* h, const float* q, uint32_t* keys);
+
+/* Text of the last error on this thread. */
+const char* aes_last_error(void);
+
+/* Host-only (no device): quantise and pack a CSR sorted by (row, col) exactly as
+ * aes_create_csr does and return the Ultra-CSR packets in reference order (partition by
+ * partition, 64 bytes each, the layout Q_packet_coo_partition + Q_write_block_x/y/val write:
+ * host_spmv_ucsr.cpp:388-425, fpga_utils.hpp:438-503).  Pass packets == NULL to learn
+ * *n_packets.  tile_rowbase (may be NULL) receives ceil(n_packets/32)+1 prefix counts of row
+ * flags per 32-packet tile. */
+int aes_pack_host(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                  uint32_t cols, const aes_params* p, uint8_t* packets, uint64_t cap_packets,
+                  uint64_t* n_packets, uint32_t* tile_rowbase);
+
+/* ---- seeded synthetic matrices (the reference matrices are not shipped) ------------------ */
+#define AES_GEN_UNIFORM_DEG 0 /* degree U{p0..p1}, distinct uniform columns, values U(0,1) */
+#define AES_GEN_FIXED_ABSNORMAL 1 /* degree p0, distinct uniform columns, values |N(0,1)| */
+#define AES_GEN_GAMMA_DEG 2   /* degree min(p1, max(1, round(Gamma(2, p0/2)))), values U(0,1) */
+#define AES_GEN_FIXED_UNIFORM 3 /* degree p0, distinct uniform columns, values U(0,1) */
+/* Pass ptr == NULL to get the total nnz only; then call again with arrays of that size.
+ * Output is a CSR sorted by (row, col).  Deterministic for (kind, rows, cols, p0, p1, seed)
+ * whatever the thread count.  Returns nnz, or (uint64_t)-1 on bad arguments. */
+uint64_t aes_gen_matrix(uint32_t kind, uint32_t rows, uint32_t cols, double p0, double p1,
+                        uint64_t seed, uint64_t* ptr, uint32_t* col, float* val);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

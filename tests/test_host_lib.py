@@ -1,0 +1,145 @@
+"""CPU tests of the C-ABI library: it loads, exports every declared entry point, and its host
+logic (generator, quantiser + Ultra-CSR packer) matches the oracle byte for byte.  No GPU."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from acceles_gb300 import engine as E
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(REPO, "include", "acceles.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(aes_[a-z_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = E.load()
+    decl = declared_symbols()
+    assert set(decl) == set(E.EXPORTS)
+    for name in decl:
+        assert hasattr(L, name), name
+
+
+def test_generator_deterministic_and_sorted():
+    a = E.gen_matrix(E.GEN_UNIFORM_DEG, 2000, 1024, 10, 30, seed=7)
+    b = E.gen_matrix(E.GEN_UNIFORM_DEG, 2000, 1024, 10, 30, seed=7)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    ptr, col, val = a
+    deg = np.diff(ptr.astype(np.int64))
+    assert deg.min() >= 10 and deg.max() <= 30
+    for r in range(0, 2000, 97):
+        c = col[ptr[r]:ptr[r + 1]]
+        assert np.all(np.diff(c.astype(np.int64)) > 0)  # distinct, sorted
+    assert val.min() >= 0.0 and val.max() < 1.0
+    g = E.gen_matrix(E.GEN_GAMMA_DEG, 5000, 1024, 32, 512, seed=3)
+    d = np.diff(g[0].astype(np.int64))
+    assert d.min() >= 1 and d.max() <= 512 and 25 < d.mean() < 40
+    n = E.gen_matrix(E.GEN_FIXED_ABSNORMAL, 300, 500, 69, 0, seed=1)
+    assert np.all(np.diff(n[0].astype(np.int64)) == 69) and n[2].min() >= 0
+
+
+def _packer_case(rows, cols, kind, p0, p1, bits, quant, seed, parts=32):
+    ptr, col, val = E.gen_matrix(kind, rows, cols, p0, p1, seed=seed)
+    pk, trb = E.pack_host(ptr, col, val, rows, cols, bits=bits, quant=quant, pack_parts=parts)
+    m = orc.Matrix(rows, cols, ptr, col, val, bits, quant, parts=parts)
+    ref = m.packets()
+    assert pk.shape == ref.shape
+    assert np.array_equal(pk, ref)
+    # tile row bases are prefix counts of the flag bits
+    P = orc.packet_size(bits)
+    flags = np.array([orc.unpack_packet(p, bits, quant == 0)[0] for p in ref], dtype=object)
+    nf = np.array([bin(int(f)).count("1") for f in flags], np.int64)
+    tiles = (len(ref) + 31) // 32
+    pref = np.concatenate([[0], np.cumsum([nf[t * 32:(t + 1) * 32].sum() for t in range(tiles)])])
+    assert np.array_equal(trb.astype(np.int64), pref)
+    assert pref[-1] == rows - 1
+    return m, ref
+
+
+@pytest.mark.parametrize("bits", [4, 6, 8])
+@pytest.mark.parametrize("quant", [0, 1, 2])
+def test_packer_matches_oracle(bits, quant):
+    _packer_case(1000, 1024, E.GEN_UNIFORM_DEG, 10, 30, bits, quant, seed=bits * 10 + quant)
+
+
+def test_packer_ragged_partitions_and_long_rows():
+    # rows not divisible by 32, rows spanning many packets and tiles, tiny partitions
+    _packer_case(77, 1024, E.GEN_GAMMA_DEG, 200, 1024, 6, 0, seed=5)
+    _packer_case(5, 64, E.GEN_FIXED_UNIFORM, 64, 0, 8, 0, seed=6)
+    _packer_case(1, 1024, E.GEN_FIXED_UNIFORM, 1024, 0, 4, 2, seed=9, parts=1)
+
+
+def test_packer_decodes_back_to_quantised_csr():
+    rows, cols, bits = 300, 700, 6
+    ptr, col, val = E.gen_matrix(E.GEN_UNIFORM_DEG, rows, cols, 1, 40, seed=11)
+    m = orc.Matrix(rows, cols, ptr, col, val, bits, 0)
+    ref = m.packets()
+    P = orc.packet_size(bits)
+    rowc, colc, valc = [], [], []
+    base = 0
+    first = True
+    for p in ref:
+        f, c, v = orc.unpack_packet(p, bits, True)
+        ctr = orc.xdecode(f, P, base)
+        base = int(ctr[-1])
+        for j in range(P):
+            if v[j] == 0 and c[j] == 0 and not (f >> j) & 1:
+                continue  # tail slot
+            rowc.append(int(ctr[j]))
+            colc.append(int(c[j]))
+            valc.append(int(v[j]))
+    qrow = np.repeat(np.arange(rows), np.diff(m.qptr.astype(np.int64)))
+    assert np.array_equal(np.array(rowc), qrow)
+    assert np.array_equal(np.array(colc), m.qcol)
+    assert np.array_equal(np.array(valc), m.qval)
+
+
+def test_packet_known_answer():
+    """Two rows, hand-computed bit positions for B=6 (P=30): flags at bits [0,30), columns at
+    [30+10j, ...), values at [330+6j, ...)."""
+    ptr = np.array([0, 2, 3], np.uint64)
+    col = np.array([5, 1023, 7], np.uint32)
+    val = np.array([1.0, -0.5, 0.25], np.float32)
+    pk, _ = E.pack_host(ptr, col, val, 2, 1024, bits=6, quant=0, pack_parts=1)
+    assert pk.shape == (1, 64)
+    bits = np.unpackbits(pk[0], bitorder="little")
+    # scale m = 1.0, M = 31: values 31, round(-15.5) = -16 (half to even), round(7.75) = 8
+    assert list(bits[:3]) == [0, 0, 1]                     # row flags
+    def field(pos, w):
+        return int(sum(int(bits[pos + i]) << i for i in range(w)))
+    assert field(30, 10) == 5 and field(40, 10) == 1023 and field(50, 10) == 7
+    assert field(330, 6) == 31 and field(336, 6) == (-16) & 63 and field(342, 6) == 8
+    assert bits[348:].sum() == 0 and bits[3:30].sum() == 0
+
+
+def test_invalid_arguments_return_codes():
+    ptr = np.array([0, 1], np.uint64)
+    col = np.array([0], np.uint32)
+    val = np.array([1.0], np.float32)
+    with pytest.raises(E.AesError) as ei:
+        E.pack_host(ptr, col, val, 1, 2048, bits=6)
+    assert ei.value.code == E.AES_ERR_UNSUPPORTED
+    with pytest.raises(E.AesError) as ei:
+        E.pack_host(ptr, col, val, 1, 4, bits=5)
+    assert ei.value.code == E.AES_ERR_UNSUPPORTED
+    with pytest.raises(E.AesError) as ei:
+        E.pack_host(ptr, col, -val, 1, 4, bits=6, quant=1)
+    assert ei.value.code == E.AES_ERR_INVALID
+    with pytest.raises(E.AesError):
+        E.pack_host(ptr, np.array([9], np.uint32), val, 1, 4, bits=6)
+
+
+def test_create_without_gpu_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(E.AesError) as ei:
+        E.SpMV(2, 4, row=[0, 1], col=[0, 1], val=[1.0, 1.0])
+    assert ei.value.code in (E.AES_ERR_NODEV, E.AES_ERR_CUDA)
