@@ -114,6 +114,13 @@ struct Engine {
   cudaStream_t last_stream = nullptr;
   bool ran = false;
 
+  // profiling / counters
+  uint64_t n_launch = 0, n_cand = 0, n_repaired = 0;
+  std::vector<cudaEvent_t> prof_ev;  // pairs
+  size_t prof_used = 0;
+  double prof_ms = 0.0;
+  uint64_t prof_n = 0;
+
   int plain_grid = 0;
   size_t plain_smem = 0, final_smem = 0;
   size_t bytes = 0;
@@ -123,6 +130,8 @@ struct Engine {
 
   void release() {
     if (device >= 0) cudaSetDevice(device);
+    for (cudaEvent_t ev : prof_ev) cudaEventDestroy(ev);
+    prof_ev.clear();
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
     if (h_q32) cudaFreeHost(h_q32);
@@ -157,7 +166,20 @@ struct Engine {
   int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s);
+  int collect_profile();
 };
+
+int Engine::collect_profile() {
+  for (size_t i = 0; i + 1 < prof_used; i += 2) {
+    AES_CK(cudaEventSynchronize(prof_ev[i + 1]));
+    float ms = 0.0f;
+    AES_CK(cudaEventElapsedTime(&ms, prof_ev[i], prof_ev[i + 1]));
+    prof_ms += ms;
+    prof_n++;
+  }
+  prof_used = 0;
+  return AES_OK;
+}
 
 int Engine::build(const HostCSR& m, const aes_params& p) {
   prm = p;
@@ -373,8 +395,30 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
   int grid = plain_grid;
   if (mode == MODE_SAMPLE) grid = std::min<int>(grid, (int)((n_sample_tiles + kWarpsPlain - 1) / kWarpsPlain));
   grid = std::max(grid, 1);
+  const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
+  if (prof) {
+    if (prof_used + 2 > prof_ev.size()) {
+      if (prof_ev.size() >= 8192) {
+        int rc = collect_profile();
+        if (rc) return rc;
+      } else {
+        for (int i = 0; i < 256; i++) {
+          cudaEvent_t ev;
+          AES_CK(cudaEventCreate(&ev));
+          prof_ev.push_back(ev);
+        }
+      }
+    }
+    AES_CK(cudaEventRecord(prof_ev[prof_used], s));
+  }
   pick_plain((int)bits, sgn, mode)<<<grid, kThreadsPlain, plain_smem, s>>>(a);
   AES_CK(cudaGetLastError());
+  if (prof) {
+    AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
+    prof_used += 2;
+  }
+  n_launch++;
+  if (mode != MODE_SAMPLE) n_cand++;
   return AES_OK;
 }
 
@@ -384,6 +428,7 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   k_quantize<<<nq, 256, 0, s>>>(d_q, cols, ld32, (int)bits, (int)quant,
                                 (int)prm.query_quant, d_q8, ld8, d_status);
   AES_CK(cudaGetLastError());
+  n_launch += 4;  // quantise, threshold, select, final
   for (uint32_t q = 0; q < nq; q++) {
     int rc = run_plain(MODE_SAMPLE, q, s);
     if (rc) return rc;
@@ -441,6 +486,8 @@ int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cud
   for (uint32_t q = 0; q < nq; q++) {
     if (!(h_status[q] & (ST_OVERFLOW | ST_MISS))) continue;
     nrep++;
+    n_repaired++;
+    n_launch += 2;
     int rc = run_plain(MODE_ALL, q, s);
     if (rc) return rc;
     SelectArgs sa{};
@@ -707,6 +754,24 @@ int aes_finish(aes_handle* h, uint32_t* repaired) {
   int rc = e.repair(e.last_nq, e.last_k, e.last_idx, e.last_score, e.last_stream, repaired);
   e.last_from_device = false;
   return rc;
+}
+
+int aes_get_stats(aes_handle* h, aes_stats* st, int reset) {
+  if (!h || !st) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  cudaSetDevice(e.device);
+  int rc = e.collect_profile();
+  if (rc) return rc;
+  st->launches = e.n_launch;
+  st->cand_launches = e.n_cand;
+  st->cand_ms = e.prof_ms;
+  st->cand_timed = e.prof_n;
+  st->repaired = e.n_repaired;
+  if (reset) {
+    e.n_launch = e.n_cand = e.n_repaired = e.prof_n = 0;
+    e.prof_ms = 0.0;
+  }
+  return AES_OK;
 }
 
 int aes_score_all(aes_handle* h, const float* q, uint32_t* keys) {

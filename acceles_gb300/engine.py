@@ -40,7 +40,9 @@ GEN_FIXED_UNIFORM = 3
 
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
            "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
-           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all"]
+           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats"]
+
+FLAG_PROFILE = 1
 
 
 class AesError(RuntimeError):
@@ -57,6 +59,12 @@ class Params(ctypes.Structure):
                 ("sample_stride", ctypes.c_uint32), ("batch_tile", ctypes.c_uint32),
                 ("device", ctypes.c_int32), ("flags", ctypes.c_uint32),
                 ("seed", ctypes.c_uint64), ("mem_limit", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_uint64), ("cand_launches", ctypes.c_uint64),
+                ("cand_ms", ctypes.c_double), ("cand_timed", ctypes.c_uint64),
+                ("repaired", ctypes.c_uint64)]
 
 
 class Info(ctypes.Structure):
@@ -129,6 +137,8 @@ def load(build_if_missing: bool = True):
     L.aes_pack_host.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.POINTER(Params), ctypes.c_void_p, ctypes.c_uint64, _u64p,
                                 _u32p]
+    L.aes_get_stats.restype = ctypes.c_int
+    L.aes_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats), ctypes.c_int]
     L.aes_score_all.restype = ctypes.c_int
     L.aes_score_all.argtypes = [ctypes.c_void_p, _f32p, _u32p]
     _lib = L
@@ -276,6 +286,11 @@ class SpMV:
         keys = np.zeros(self.rows, np.uint32)
         _check(load().aes_score_all(self._h, _p(q, _f32p), _p(keys, _u32p)))
         return keys
+
+    def stats(self, reset=True):
+        st = Stats()
+        _check(load().aes_get_stats(self._h, ctypes.byref(st), 1 if reset else 0))
+        return {f: getattr(st, f) for f, _ in st._fields_}
 
     def info(self):
         inf = Info()

@@ -66,6 +66,17 @@ typedef struct aes_params {
   uint64_t mem_limit;     /* device bytes this handle may allocate; 0 = no limit */
 } aes_params;
 
+/* params.flags bits */
+#define AES_FLAG_PROFILE 1u /* time every candidate-pass launch with CUDA events on its stream */
+
+typedef struct aes_stats {
+  uint64_t launches;       /* kernels launched by the engine since the last reset */
+  uint64_t cand_launches;  /* full-matrix candidate-pass launches (the dominant kernel) */
+  double cand_ms;          /* device time of those launches (AES_FLAG_PROFILE only) */
+  uint64_t cand_timed;     /* launches included in cand_ms */
+  uint64_t repaired;       /* queries sent down the exact slow path */
+} aes_stats;
+
 typedef struct aes_info {
   uint32_t rows, cols, bits, packet_elems;
   uint64_t nnz, quantized_nnz, packets, tiles;
@@ -129,6 +140,10 @@ int aes_finish(aes_handle* h, uint32_t* repaired);
  * AES_QUANT_UNSIGNED_ROW.  Synchronous.  The integer counterpart of the reference's full SpMV
  * check (spmv_coo_gold4 + sort_pr in sw_test, host_spmv_ucsr.cpp:841-869). */
 int aes_score_all(aes_handle* h, const float* q, uint32_t* keys);
+
+/* Counters since the previous call (reset = 1 clears them).  Waits for the handle's pending
+ * timing events. */
+int aes_get_stats(aes_handle* h, aes_stats* st, int reset);
 
 /* Text of the last error on this thread. */
 const char* aes_last_error(void);

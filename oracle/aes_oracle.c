@@ -479,3 +479,98 @@ uint32_t orc_two_stage(const uint64_t* ptr, const uint32_t* col, const float* va
   free(q); free(s); free(keys); free(sc); free(ix);
   return nout;
 }
+
+/* ---------------------------------------------------------------------------------------- */
+/* CPU timing harness (the reference two-stage method on host threads)                       */
+/* ---------------------------------------------------------------------------------------- */
+#include <pthread.h>
+#include <time.h>
+
+typedef struct {
+  const uint64_t* qptr;
+  const uint32_t* qcol;
+  const int32_t* qval;
+  const int32_t* q;
+  uint32_t r0, r1;
+  int k;
+  uint32_t* idx;
+  int32_t* val;
+} orc_job_t;
+
+/* streaming Top-k of gold_algorithms.hpp:249-308 over the rows [r0, r1) of a quantised CSR */
+static void* orc_job_run(void* arg) {
+  orc_job_t* j = (orc_job_t*)arg;
+  for (int i = 0; i < j->k; i++) { j->idx[i] = 0; j->val[i] = 0; }
+  int wi = 0;
+  int32_t wv = 0;
+  for (uint32_t r = j->r0; r < j->r1; r++) {
+    int32_t s = 0;
+    for (uint64_t e = j->qptr[r]; e < j->qptr[r + 1]; e++) s += j->qval[e] * j->q[j->qcol[e]];
+    if (s >= wv) {
+      j->idx[wi] = r;
+      j->val[wi] = s;
+      int bi = 0;
+      int32_t bv = j->val[0];
+      for (int t = 0; t < j->k; t++)
+        if (j->val[t] < bv) { bi = t; bv = j->val[t]; }
+      wi = bi;
+      wv = bv;
+    }
+  }
+  return NULL;
+}
+
+static double orc_now(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+double orc_bench_two_stage(const uint64_t* ptr, const uint32_t* col, const float* val,
+                           const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                           uint32_t rows, uint32_t cols, int bits, uint32_t ck, uint32_t k,
+                           const float* queries, uint32_t nq, int nthreads, double max_seconds,
+                           uint32_t* done, uint32_t* out_idx) {
+  if (nthreads < 1) nthreads = 1;
+  int32_t* q = (int32_t*)malloc(sizeof(int32_t) * cols);
+  orc_job_t* jobs = (orc_job_t*)malloc(sizeof(orc_job_t) * nthreads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+  uint32_t* cidx = (uint32_t*)malloc(sizeof(uint32_t) * ck * nthreads);
+  int32_t* cval = (int32_t*)malloc(sizeof(int32_t) * ck * nthreads);
+  comp_t* cc = (comp_t*)malloc(sizeof(comp_t) * ck * nthreads);
+  uint32_t* sel = (uint32_t*)malloc(sizeof(uint32_t) * ck);
+  float* sc = (float*)malloc(sizeof(float) * ck);
+  double t0 = orc_now();
+  uint32_t n = 0;
+  for (; n < nq; n++) {
+    if (n > 0 && orc_now() - t0 > max_seconds) break;
+    const float* x = queries + (size_t)n * cols;
+    orc_quantize_query(x, cols, bits, ORC_QUANT_SYM_GLOBAL, ORC_QQ_NUMPY, q);
+    for (int t = 0; t < nthreads; t++) {
+      jobs[t].qptr = qptr; jobs[t].qcol = qcol; jobs[t].qval = qval; jobs[t].q = q;
+      jobs[t].r0 = (uint32_t)((uint64_t)rows * t / nthreads);
+      jobs[t].r1 = (uint32_t)((uint64_t)rows * (t + 1) / nthreads);
+      jobs[t].k = (int)ck;
+      jobs[t].idx = cidx + (size_t)t * ck;
+      jobs[t].val = cval + (size_t)t * ck;
+      if (nthreads == 1) orc_job_run(&jobs[t]);
+      else pthread_create(&th[t], NULL, orc_job_run, &jobs[t]);
+    }
+    if (nthreads > 1)
+      for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    uint32_t m = ck * (uint32_t)nthreads;
+    for (uint32_t i = 0; i < m; i++)
+      cc[i].comp = ((uint64_t)orc_key_i32(cval[i]) << 32) | cidx[i];
+    qsort(cc, m, sizeof(comp_t), cmp_comp_desc);
+    uint32_t nsel = m < ck ? m : ck;
+    for (uint32_t i = 0; i < nsel; i++) sel[i] = (uint32_t)(cc[i].comp & 0xFFFFFFFFu);
+    orc_rescore_f32(ptr, col, val, x, sel, nsel, sc);
+    orc_sort_tuples_f32(nsel, sel, sc);
+    if (out_idx)
+      for (uint32_t i = 0; i < k && i < nsel; i++) out_idx[(size_t)n * k + i] = sel[i];
+  }
+  double el = orc_now() - t0;
+  *done = n;
+  free(q); free(jobs); free(th); free(cidx); free(cval); free(cc); free(sel); free(sc);
+  return el;
+}

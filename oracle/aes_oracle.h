@@ -124,6 +124,19 @@ uint32_t orc_two_stage(const uint64_t* ptr, const uint32_t* col, const float* va
                        int qq, uint32_t split, uint32_t ck, uint32_t k, const float* query,
                        uint32_t* out_idx, float* out_score, uint32_t* cand, uint32_t* cand_n);
 
+/* ---- CPU timing harness ------------------------------------------------------------------- */
+/* The two-stage method for up to nq queries on nthreads host threads (symmetric quantiser):
+ * each thread runs the streaming Top-CK of gold_algorithms.hpp:249-308 over its row block, the
+ * blocks' candidates merge to the Top-CK by (key desc, row desc), then FP32 rescoring and
+ * sort_tuples.  Stops once max_seconds have passed (after at least one query).  Returns the
+ * elapsed seconds, timed through the thread joins; *done = queries completed; out_idx (may be
+ * NULL) receives [done][k] result rows. */
+double orc_bench_two_stage(const uint64_t* ptr, const uint32_t* col, const float* val,
+                           const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                           uint32_t rows, uint32_t cols, int bits, uint32_t ck, uint32_t k,
+                           const float* queries, uint32_t nq, int nthreads, double max_seconds,
+                           uint32_t* done, uint32_t* out_idx);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,12 @@ def lib():
                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
                                     ctypes.c_uint32, _f32p, _u32p, _f32p, _u32p, _u32p]
+        L.orc_bench_two_stage.restype = ctypes.c_double
+        L.orc_bench_two_stage.argtypes = [_u64p, _u32p, _f32p, _u64p, _u32p, _i32p,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.c_uint32, ctypes.c_uint32, _f32p,
+                                          ctypes.c_uint32, ctypes.c_int, ctypes.c_double, _u32p,
+                                          _u32p]
         _lib = L
     return _lib
 
@@ -333,6 +339,19 @@ class Matrix:
                                 self.bits, self.quant, qq, split, ck, k, _p(q, _f32p),
                                 _p(oi, _u32p), _p(os_, _f32p), _p(cand, _u32p), _p(cn, _u32p))
         return oi[:n].copy(), os_[:n].copy(), cand[: int(cn[0])].copy()
+
+
+def bench_two_stage(m: "Matrix", queries, ck, k, nthreads=1, max_seconds=10.0):
+    """Time the CPU two-stage method (symmetric quantiser) on host threads.
+    Returns (seconds, queries done, result rows [done, k])."""
+    Q = np.ascontiguousarray(queries, np.float32)
+    done = np.zeros(1, np.uint32)
+    out = np.zeros((Q.shape[0], k), np.uint32)
+    el = lib().orc_bench_two_stage(_p(m.ptr, _u64p), _p(m.col, _u32p), _p(m.val, _f32p),
+                                   _p(m.qptr, _u64p), _p(m.qcol, _u32p), _p(m.qval, _i32p),
+                                   m.rows, m.cols, m.bits, ck, k, _p(Q, _f32p), Q.shape[0],
+                                   nthreads, max_seconds, _p(done, _u32p), _p(out, _u32p))
+    return el, int(done[0]), out[: int(done[0])]
 
 
 # ---------------------------------------------------------------------------------------------
