@@ -1,0 +1,288 @@
+// aes_batch.cuh -- batched candidate pass: one read of the Ultra-CSR matrix scores a tile of up
+// to 128 queries (the reference's spmv_ucsr_top_k_main scores one query per pass,
+// spmv_ucsr_top_k_multicore.cpp:8-143).
+//
+// Per warp and 32-packet tile:
+//   phase A (lane = packet): decode the packet's flags, 10-bit columns and B-bit values into
+//            per-warp shared records in element order;
+//   phase B (lane = 4 queries): walk the tile's elements four at a time.  For a group of four
+//            elements every lane gathers its four queries' bytes at the four columns (one 32-bit
+//            load each from qtab[col][128]), transposes the 4x4 bytes with PRMT and accumulates
+//            with dp4a (exact int8 x int8 -> int32).  Row flags are the same for every lane,
+//            so row boundaries never diverge.
+#pragma once
+
+#include "aes_kernels.cuh"
+
+namespace aes {
+namespace dev {
+
+constexpr int kBatchQ = 128;         // queries per tile (32 lanes x 4)
+constexpr int kWarpsBatchMax = 16;
+constexpr size_t kSmemMax = 227 * 1024;
+
+struct BatchArgs {
+  const uint4* tiles;
+  const uint32_t* tile_rowbase;
+  uint32_t n_tiles, n_rows, cols;
+  const uint32_t* qtab;         // [cols][32] words: bytes of queries 4l..4l+3 at (col, lane l)
+  uint32_t q0, nq;              // this launch scores queries q0 .. q0 + nq - 1 (nq <= 128)
+  const float* rowscale;
+  uint32_t split, slice;
+  const uint32_t* thr;          // [nq_total][split] (MODE_FILTER)
+  uint32_t* cnt;                // [nq_total][split]
+  uint2* surv;                  // [nq_total][split][cap]
+  uint32_t cap;
+  uint32_t* keys_out;           // MODE_SAMPLE: [sample rows][128]
+  const uint32_t* sample_first;
+  uint32_t sample_stride, n_sample_tiles;
+};
+
+template <int B>
+__host__ __device__ constexpr size_t batch_warp_bytes() {
+  // offsets (u32) + values (u8) + flags (u8) for 32 packets
+  return (size_t)32 * packet_elems(B) * 6;
+}
+
+__host__ __device__ inline bool batch_thr_in_smem(uint32_t split) { return split > 1 && split <= 32; }
+
+// warps per CTA that fit next to the query table (and thresholds) in shared memory
+__host__ inline int batch_warps(int B, uint32_t cols, uint32_t split) {
+  const size_t per = (size_t)32 * packet_elems(B) * 6;
+  const size_t fixed = (size_t)cols * kBatchQ + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0);
+  int w = (int)((kSmemMax - fixed) / per);
+  return w > kWarpsBatchMax ? kWarpsBatchMax : w;
+}
+__host__ inline size_t batch_smem_bytes(int B, uint32_t cols, uint32_t split, int warps) {
+  const size_t per = (size_t)32 * packet_elems(B) * 6;
+  return (size_t)cols * kBatchQ + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0) +
+         (size_t)warps * per;
+}
+
+// 4x4 byte transpose: V[t] byte i = W[i] byte t
+__device__ __forceinline__ void transpose4(const uint32_t (&W)[4], uint32_t (&V)[4]) {
+  const uint32_t x0 = __byte_perm(W[0], W[1], 0x5140);
+  const uint32_t x1 = __byte_perm(W[0], W[1], 0x7362);
+  const uint32_t y0 = __byte_perm(W[2], W[3], 0x5140);
+  const uint32_t y1 = __byte_perm(W[2], W[3], 0x7362);
+  V[0] = __byte_perm(x0, y0, 0x5410);
+  V[1] = __byte_perm(x0, y0, 0x7632);
+  V[2] = __byte_perm(x1, y1, 0x5410);
+  V[3] = __byte_perm(x1, y1, 0x7632);
+}
+
+template <bool SGN>
+__device__ __forceinline__ int32_t dot4(uint32_t a, uint32_t b, int32_t c) {
+  if constexpr (SGN) return __dp4a((int)a, (int)b, c);
+  else return (int32_t)__dp4a(a, b, (unsigned)c);
+}
+
+template <int MODE>
+struct BatchRows {
+  const BatchArgs& a;
+  const uint32_t* thr_s;  // [split][128] in smem (split in 2..64), else nullptr
+  uint32_t thr4[4];       // split == 1
+  uint32_t sample_base;
+  uint32_t lane;
+
+  // the four queries of this lane finished row `row` with integer scores acc[0..3]
+  __device__ __forceinline__ void finish(uint32_t row, const int32_t (&acc)[4]) const {
+    uint32_t key[4];
+    if (a.rowscale) {
+      const float rs = __ldg(a.rowscale + row);
+#pragma unroll
+      for (int t = 0; t < 4; t++) key[t] = key_f32(__fmul_rn(__int2float_rn(acc[t]), rs));
+    } else {
+#pragma unroll
+      for (int t = 0; t < 4; t++) key[t] = key_i32(acc[t]);
+    }
+    if constexpr (MODE == MODE_SAMPLE) {
+      reinterpret_cast<uint4*>(a.keys_out)[(size_t)(row - sample_base) * 32 + lane] =
+          make_uint4(key[0], key[1], key[2], key[3]);
+    } else if constexpr (MODE == MODE_FILTER) {
+      const uint32_t p = part_of(row, a.split, a.slice);
+      uint32_t th[4];
+      if (a.split <= 1) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) th[t] = thr4[t];
+      } else if (thr_s) {
+        const uint4 v = reinterpret_cast<const uint4*>(thr_s)[p * 32 + lane];
+        th[0] = v.x; th[1] = v.y; th[2] = v.z; th[3] = v.w;
+      } else {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const uint32_t q = 4 * lane + t;
+          th[t] = q < a.nq ? __ldg(a.thr + (size_t)(a.q0 + q) * a.split + p) : 0xFFFFFFFFu;
+        }
+      }
+      const bool hit = (key[0] >= th[0]) | (key[1] >= th[1]) | (key[2] >= th[2]) | (key[3] >= th[3]);
+      if (__any_sync(0xFFFFFFFFu, hit) && hit) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const uint32_t q = 4 * lane + t;
+          if (key[t] >= th[t] && q < a.nq) {
+            const size_t qp = (size_t)(a.q0 + q) * a.split + p;
+            const uint32_t i = atomicAdd(a.cnt + qp, 1u);
+            if (i < a.cap) a.surv[qp * a.cap + i] = make_uint2(key[t], row);
+          }
+        }
+      }
+    }
+  }
+};
+
+template <int B, bool SGN, int MODE>
+__device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
+                            const BatchRows<MODE>& rows, const uint8_t* qtb,
+                            unsigned char* wsm) {
+  constexpr int P = packet_elems(B);
+  constexpr int NE = 32 * P;     // elements per tile
+  constexpr int NG = NE / 4;     // groups of four
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lane4 = lane << 2;
+  uint32_t* offs = reinterpret_cast<uint32_t*>(wsm);            // [NE] col * 128
+  uint8_t* vals = wsm + (size_t)NE * 4;                          // [NE]
+  uint8_t* flg = wsm + (size_t)NE * 5;                           // [NE]
+  if (tb >= te) return;
+  bool owned = (tb == 0);
+  uint32_t row = __ldg(a.tile_rowbase + tb);  // id of the row open before the first entry
+  int32_t acc[4] = {0, 0, 0, 0};
+  uint32_t w[16], nw[16];
+  load_tile(a.tiles, tb, lane, w);
+  for (uint32_t t = tb;; t++) {
+    if (t >= a.n_tiles) {
+      if (owned) rows.finish(row, acc);
+      return;
+    }
+    const bool closing = (t >= te);
+    if (t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
+    // ---- phase A: this lane's packet -> records ----------------------------------------------
+    {
+      using D = PacketDecoder<B, SGN>;
+      const auto F = D::flags(w);
+      uint32_t* o = offs + lane * P;
+      uint8_t* v = vals + lane * P;
+      uint8_t* f = flg + lane * P;
+#pragma unroll
+      for (int j = 0; j < P; j++) {
+        const uint32_t cpos = P + 10 * j, vpos = 11 * P + B * j;
+        const uint32_t cw = __funnelshift_r(w[cpos >> 5], w[(cpos >> 5) + 1 < 16 ? (cpos >> 5) + 1 : 15], cpos & 31);
+        o[j] = (cw & 0x3FFu) << 7;
+        const uint32_t vw = __funnelshift_r(w[vpos >> 5], w[(vpos >> 5) + 1 < 16 ? (vpos >> 5) + 1 : 15], vpos & 31);
+        uint32_t vb = vw & ((1u << B) - 1u);
+        if (SGN) vb = (uint32_t)(((int32_t)(vb << (32 - B))) >> (32 - B)) & 0xFFu;
+        v[j] = (uint8_t)vb;
+        f[j] = (uint8_t)((F >> j) & 1u);
+      }
+    }
+    __syncwarp();
+    // ---- phase B: lanes = queries ------------------------------------------------------------
+    for (int g = 0; g < NG; g++) {
+      const uint4 o4 = reinterpret_cast<const uint4*>(offs)[g];
+      const uint32_t v4 = reinterpret_cast<const uint32_t*>(vals)[g];
+      const uint32_t f4 = reinterpret_cast<const uint32_t*>(flg)[g];
+      uint32_t W[4], V[4];
+      W[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x | lane4));
+      W[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y | lane4));
+      W[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z | lane4));
+      W[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w | lane4));
+      transpose4(W, V);
+      if (f4 == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4, V[q], acc[q]);
+        continue;
+      }
+      // a row starts at one or more of the four elements: split the group at each flag
+      uint32_t lo = 0;  // first element of the group not yet accumulated
+      for (int i = 0; i < 4; i++) {
+        if (!((f4 >> (8 * i)) & 1u)) continue;
+        if (i > lo) {
+          const uint32_t m = (0xFFFFFFFFu >> (8 * (4 - i))) & (0xFFFFFFFFu << (8 * lo));
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & m, V[q], acc[q]);
+        }
+        if (owned) rows.finish(row, acc);
+        if (closing) return;
+        row++;
+        owned = true;
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q] = 0;
+        lo = i;
+      }
+      const uint32_t m = 0xFFFFFFFFu << (8 * lo);
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & m, V[q], acc[q]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 16; i++) w[i] = nw[i];
+  }
+}
+
+template <int B, bool SGN, int MODE>
+__global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint8_t* qtb = smem;                                           // [cols][128] bytes
+  uint32_t* thr_s = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * kBatchQ);
+  const bool thr_in_smem = (MODE == MODE_FILTER) && batch_thr_in_smem(a.split);
+  unsigned char* wsm_all = smem + (size_t)a.cols * kBatchQ +
+                           (batch_thr_in_smem(a.split) ? (size_t)a.split * kBatchQ * 4 : 0);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  unsigned char* wsm = wsm_all + (size_t)warp * batch_warp_bytes<B>();
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(a.qtab);
+    uint4* dst = reinterpret_cast<uint4*>(qtb);
+    for (uint32_t i = threadIdx.x; i < a.cols * (kBatchQ / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  BatchRows<MODE> rows{a, nullptr, {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, 0u, lane};
+  if constexpr (MODE == MODE_FILTER) {
+    if (thr_in_smem) {
+      for (uint32_t i = threadIdx.x; i < a.split * kBatchQ; i += blockDim.x) {
+        const uint32_t p = i / kBatchQ, q = i % kBatchQ;
+        thr_s[i] = q < a.nq ? a.thr[(size_t)(a.q0 + q) * a.split + p] : 0xFFFFFFFFu;
+      }
+      rows.thr_s = thr_s;
+    } else if (a.split <= 1) {
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const uint32_t q = 4 * lane + t;
+        rows.thr4[t] = q < a.nq ? a.thr[(size_t)(a.q0 + q) * a.split] : 0xFFFFFFFFu;
+      }
+    }
+  }
+  __syncthreads();
+  const uint32_t wpc = blockDim.x >> 5;
+  const uint32_t gw = blockIdx.x * wpc + warp;
+  const uint32_t nwp = gridDim.x * wpc;
+  if constexpr (MODE == MODE_SAMPLE) {
+    for (uint32_t s = gw; s < a.n_sample_tiles; s += nwp) {
+      const uint32_t t = s * a.sample_stride;
+      BatchRows<MODE> r2 = rows;
+      r2.sample_base = __ldg(a.sample_first + s);
+      batch_range<B, SGN, MODE>(a, t, t + 1, r2, qtb, wsm);
+    }
+  } else {
+    const uint64_t n = a.n_tiles;
+    const uint32_t tb = (uint32_t)((n * gw) / nwp), te = (uint32_t)((n * (gw + 1)) / nwp);
+    batch_range<B, SGN, MODE>(a, tb, te, rows, qtb, wsm);
+  }
+}
+
+// qtab[col][32] words: byte t of word (col, l) = quantised query q0 + 4l + t at col (0 past nq)
+__global__ void k_qtable(const int8_t* __restrict__ q8, uint32_t ld8, uint32_t cols, uint32_t q0,
+                         uint32_t nq, uint32_t* __restrict__ qtab) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cols * 32u) return;
+  const uint32_t c = i >> 5, l = i & 31u;
+  uint32_t w = 0;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    const uint32_t q = 4 * l + t;
+    const uint32_t b = q < nq ? (uint32_t)(uint8_t)q8[(size_t)(q0 + q) * ld8 + c] : 0u;
+    w |= b << (8 * t);
+  }
+  qtab[i] = w;
+}
+
+}  // namespace dev
+}  // namespace aes

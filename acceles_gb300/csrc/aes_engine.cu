@@ -18,6 +18,7 @@
 #include "acceles.h"
 #include "aes_host.hpp"
 #include "aes_kernels.cuh"
+#include "aes_batch.cuh"
 
 namespace aes {
 const char* last_error_cstr();
@@ -31,6 +32,20 @@ const char* last_error_cstr();
 using namespace dev;
 
 typedef void (*PlainKernel)(PlainArgs);
+typedef void (*BatchKernel)(BatchArgs);
+
+template <int B, bool SGN>
+static BatchKernel batch_kernel(int mode) {
+  return mode == MODE_SAMPLE ? k_cand_batch<B, SGN, MODE_SAMPLE> : k_cand_batch<B, SGN, MODE_FILTER>;
+}
+
+static BatchKernel pick_batch(int bits, bool sgn, int mode) {
+  switch (bits) {
+    case 4: return sgn ? batch_kernel<4, true>(mode) : batch_kernel<4, false>(mode);
+    case 6: return sgn ? batch_kernel<6, true>(mode) : batch_kernel<6, false>(mode);
+    default: return sgn ? batch_kernel<8, true>(mode) : batch_kernel<8, false>(mode);
+  }
+}
 
 template <int B, bool SGN>
 static PlainKernel plain_kernel(int mode) {
@@ -123,6 +138,12 @@ struct Engine {
 
   int plain_grid = 0;
   size_t plain_smem = 0, final_smem = 0;
+  // batched pass
+  uint32_t* d_qtab = nullptr;     // [blocks][cols][32] words
+  int batch_warps_n = 0, batch_grid = 0;
+  size_t batch_smem = 0;
+  uint32_t batch_mode = 0;        // 0 auto, 1 never, else always
+  bool last_batched = false;
   size_t bytes = 0;
   std::vector<void*> allocs;
 
@@ -166,6 +187,7 @@ struct Engine {
   int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s);
+  int run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s);
   int collect_profile();
 };
 
@@ -230,7 +252,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
 
   // ---- sample tiles -------------------------------------------------------------------------
   if (p.sample_stride) ss = p.sample_stride;
-  else ss = tiles <= 64 ? 1 : 64;
+  else ss = tiles <= 64 ? 1 : (tiles <= 16384 ? 64 : 256);
   n_sample_tiles = (uint32_t)((tiles + ss - 1) / ss);
   auto owned_begin = [&](uint64_t t) -> uint64_t {
     if (t >= tiles) return rows;
@@ -293,9 +315,11 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   plan += (quant == AES_QUANT_UNSIGNED_ROW) ? rows * 4ull : 0;
   plan += (rows + 1) * 4ull + nnz * 6ull;
   plan += (n_sample_tiles + 2ull * split + 2) * 4;
-  plan += (size_t)maxB * (ld32 * 4ull + ld8 + (size_t)n_sample_rows * 4 + split * 8ull +
+  plan += (size_t)((maxB + kBatchQ - 1) / kBatchQ) * kBatchQ * (size_t)n_sample_rows * 4;
+  plan += (size_t)maxB * (ld32 * 4ull + ld8 + split * 8ull +
                           (size_t)split * cap * 8 + nslots * 8ull + 4 + p.k_max * 8ull);
   plan += rows * 4ull;  // slow-path key array
+  plan += (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 128;
   if (p.mem_limit && plan > p.mem_limit)
     return fail(AES_ERR_NOMEM, "matrix needs " + std::to_string(plan) +
                                    " device bytes, over the handle limit " +
@@ -319,7 +343,9 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_AL(d_part_r, split);
   AES_AL(d_q32, (size_t)maxB * ld32);
   AES_AL(d_q8, (size_t)maxB * ld8);
-  AES_AL(d_sample_keys, (size_t)maxB * std::max<uint32_t>(n_sample_rows, 1));
+  // batched passes write sample keys per block of kBatchQ queries: pad to whole blocks
+  const size_t maxB_blk = (size_t)((maxB + kBatchQ - 1) / kBatchQ) * kBatchQ;
+  AES_AL(d_sample_keys, maxB_blk * std::max<uint32_t>(n_sample_rows, 1));
   AES_AL(d_thr, (size_t)maxB * split);
   AES_AL(d_cnt, (size_t)maxB * split);
   AES_AL(d_surv, (size_t)maxB * split * cap);
@@ -329,6 +355,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_AL(d_out_idx, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_allkeys, rows);
+  AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 32);
 #undef AES_AL
   AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
   AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
@@ -355,7 +382,11 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_CK(cudaMemset(d_q32, 0, (size_t)maxB * ld32 * 4));
 
   // ---- launch geometry ---------------------------------------------------------------------
-  plain_smem = (size_t)cols * 128 + (size_t)kWarpsPlain * (P - 1) * 32 * 4;
+  {
+    size_t stage = (size_t)((P + 3) / 4) * 32 * 16;
+    plain_smem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
+                 (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
+  }
   for (int mode = 0; mode < 3; mode++) {
     PlainKernel kf = pick_plain((int)bits, sgn, mode);
     AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -365,6 +396,21 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), kThreadsPlain, plain_smem));
   plain_grid = std::max(1, occ) * sm_count;
+  batch_mode = p.batch_tile;
+  batch_warps_n = batch_warps((int)bits, cols, split);
+  if (batch_warps_n < 1) batch_mode = 1;  // query table does not fit: plain passes only
+  if (batch_mode != 1) {
+    batch_smem = batch_smem_bytes((int)bits, cols, split, batch_warps_n);
+    for (int mode = 0; mode < 2; mode++) {
+      BatchKernel kf = pick_batch((int)bits, sgn, mode);
+      AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)batch_smem));
+    }
+    int occb = 0;
+    AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occb, (const void*)pick_batch((int)bits, sgn, MODE_FILTER), batch_warps_n * 32, batch_smem));
+    batch_grid = std::max(1, occb) * sm_count;
+  }
   final_smem = ((cols * 4 + 15) & ~15u) + (size_t)npow2 * 8;
   AES_CK(cudaFuncSetAttribute((const void*)k_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)final_smem));
@@ -422,6 +468,58 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
   return AES_OK;
 }
 
+int Engine::run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
+  BatchArgs a{};
+  a.tiles = d_tiles;
+  a.tile_rowbase = d_tile_rowbase;
+  a.n_tiles = (uint32_t)tiles;
+  a.n_rows = rows;
+  a.cols = cols;
+  a.qtab = d_qtab + (size_t)blk * cols * 32;
+  a.q0 = blk * kBatchQ;
+  a.nq = nq_blk;
+  a.rowscale = d_rowscale;
+  a.split = split;
+  a.slice = slice;
+  a.thr = d_thr;
+  a.cnt = d_cnt;
+  a.surv = d_surv;
+  a.cap = cap;
+  a.keys_out = d_sample_keys + (size_t)blk * kBatchQ * n_sample_rows;
+  a.sample_first = d_sample_first;
+  a.sample_stride = ss;
+  a.n_sample_tiles = n_sample_tiles;
+  int grid = batch_grid;
+  if (mode == MODE_SAMPLE)
+    grid = std::min<int>(grid, (int)((n_sample_tiles + batch_warps_n - 1) / batch_warps_n));
+  grid = std::max(grid, 1);
+  const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
+  if (prof) {
+    if (prof_used + 2 > prof_ev.size()) {
+      if (prof_ev.size() >= 8192) {
+        int rc = collect_profile();
+        if (rc) return rc;
+      } else {
+        for (int i = 0; i < 256; i++) {
+          cudaEvent_t ev;
+          AES_CK(cudaEventCreate(&ev));
+          prof_ev.push_back(ev);
+        }
+      }
+    }
+    AES_CK(cudaEventRecord(prof_ev[prof_used], s));
+  }
+  pick_batch((int)bits, sgn, mode)<<<grid, batch_warps_n * 32, batch_smem, s>>>(a);
+  AES_CK(cudaGetLastError());
+  if (prof) {
+    AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
+    prof_used += 2;
+  }
+  n_launch++;
+  if (mode != MODE_SAMPLE) n_cand++;
+  return AES_OK;
+}
+
 int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
                     cudaStream_t s) {
   AES_CK(cudaMemsetAsync(d_status, 0, nq * 4ull, s));
@@ -429,16 +527,39 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
                                 (int)prm.query_quant, d_q8, ld8, d_status);
   AES_CK(cudaGetLastError());
   n_launch += 4;  // quantise, threshold, select, final
-  for (uint32_t q = 0; q < nq; q++) {
-    int rc = run_plain(MODE_SAMPLE, q, s);
-    if (rc) return rc;
+  const bool batched = batch_mode != 1 && (batch_mode != 0 || nq >= 16);
+  last_batched = batched;
+  const uint32_t nblk = (nq + kBatchQ - 1) / kBatchQ;
+  if (batched) {
+    for (uint32_t b = 0; b < nblk; b++) {
+      const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
+      k_qtable<<<(cols * 32 + 255) / 256, 256, 0, s>>>(d_q8, ld8, cols, b * kBatchQ, nb,
+                                                       d_qtab + (size_t)b * cols * 32);
+      AES_CK(cudaGetLastError());
+      n_launch++;
+      int rc = run_batch(MODE_SAMPLE, b, nb, s);
+      if (rc) return rc;
+    }
+  } else {
+    for (uint32_t q = 0; q < nq; q++) {
+      int rc = run_plain(MODE_SAMPLE, q, s);
+      if (rc) return rc;
+    }
   }
-  k_threshold<<<dim3(split, nq), 512, 0, s>>>(d_sample_keys, n_sample_rows, d_part_sample_begin,
-                                              split, d_part_r, d_thr, d_cnt);
+  k_threshold<<<dim3(split, nq), 512, 0, s>>>(d_sample_keys, n_sample_rows, batched ? kBatchQ : 0,
+                                              d_part_sample_begin, split, d_part_r, d_thr, d_cnt);
   AES_CK(cudaGetLastError());
-  for (uint32_t q = 0; q < nq; q++) {
-    int rc = run_plain(MODE_FILTER, q, s);
-    if (rc) return rc;
+  if (batched) {
+    for (uint32_t b = 0; b < nblk; b++) {
+      const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
+      int rc = run_batch(MODE_FILTER, b, nb, s);
+      if (rc) return rc;
+    }
+  } else {
+    for (uint32_t q = 0; q < nq; q++) {
+      int rc = run_plain(MODE_FILTER, q, s);
+      if (rc) return rc;
+    }
   }
   SelectArgs sa{};
   sa.surv = d_surv;
@@ -674,7 +795,7 @@ int aes_get_info(const aes_handle* h, aes_info* info) {
   info->sample_tiles = e.n_sample_tiles;
   info->sample_rows = e.n_sample_rows;
   info->max_batch = e.maxB;
-  info->batch_tile = 1;
+  info->batch_tile = e.batch_mode == 1 ? 1 : aes::dev::kBatchQ;
   return AES_OK;
 }
 

@@ -17,10 +17,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace aes {
 namespace dev {
 
-constexpr int kWarpsPlain = 16;      // warps per CTA of the plain candidate pass
+constexpr int kWarpsPlain = 32;      // warps per CTA of the plain candidate pass
 constexpr int kThreadsPlain = kWarpsPlain * 32;
 
 enum Mode : int { MODE_FILTER = 0, MODE_SAMPLE = 1, MODE_ALL = 2 };
@@ -82,30 +84,43 @@ struct PlainArgs {
   uint32_t sample_stride, n_sample_tiles;
 };
 
+constexpr uint32_t kThrSmemMax = 4096;  // thresholds of up to this many partitions in smem
+
 __device__ __forceinline__ uint32_t part_of(uint32_t row, uint32_t split, uint32_t slice) {
   if (split <= 1) return 0;
   uint32_t p = slice ? row / slice : split - 1;
   return p < split - 1 ? p : split - 1;
 }
 
+// Where a completed row goes: the survivor buffer (filter), the sample key array, or the
+// full key array.
 template <int MODE>
-__device__ __forceinline__ void emit_row(const PlainArgs& a, uint32_t row, int32_t score,
-                                         uint32_t sample_tile) {
-  uint32_t key;
-  if (a.rowscale) key = key_f32(__fmul_rn(__int2float_rn(score), __ldg(a.rowscale + row)));
-  else key = key_i32(score);
-  if constexpr (MODE == MODE_FILTER) {
-    uint32_t p = part_of(row, a.split, a.slice);
-    if (key >= __ldg(a.thr + p)) {
-      uint32_t i = atomicAdd(a.cnt + p, 1u);
-      if (i < a.cap) a.surv[(size_t)p * a.cap + i] = make_uint2(key, row);
+struct Emitter {
+  const PlainArgs& a;
+  const uint32_t* thr_s;  // shared copy of the thresholds (split > 1)
+  uint32_t thr0;          // threshold when split == 1
+  uint32_t sample_base;   // MODE_SAMPLE: first owned row minus its key index
+  __device__ __forceinline__ void operator()(uint32_t row, int32_t score) const {
+    uint32_t key;
+    if (a.rowscale) key = key_f32(__fmul_rn(__int2float_rn(score), __ldg(a.rowscale + row)));
+    else key = key_i32(score);
+    if constexpr (MODE == MODE_FILTER) {
+      uint32_t p = 0, th = thr0;
+      if (a.split > 1) {
+        p = part_of(row, a.split, a.slice);
+        th = (a.split <= kThrSmemMax) ? thr_s[p] : __ldg(a.thr + p);
+      }
+      if (key >= th) {
+        uint32_t i = atomicAdd(a.cnt + p, 1u);
+        if (i < a.cap) a.surv[(size_t)p * a.cap + i] = make_uint2(key, row);
+      }
+    } else if constexpr (MODE == MODE_SAMPLE) {
+      a.keys_out[row - sample_base] = key;
+    } else {
+      a.keys_out[row] = key;
     }
-  } else if constexpr (MODE == MODE_SAMPLE) {
-    a.keys_out[row - __ldg(a.sample_first + sample_tile)] = key;
-  } else {
-    a.keys_out[row] = key;
   }
-}
+};
 
 __device__ __forceinline__ void load_tile(const uint4* tiles, uint32_t t, uint32_t lane,
                                           uint32_t (&w)[16]) {
@@ -120,39 +135,64 @@ __device__ __forceinline__ void load_tile(const uint4* tiles, uint32_t t, uint32
   }
 }
 
-// Per-lane decode of one packet: prefix sums S_j of val_j * q[col_j] (int32, wrapping), S_j
-// for j < P-1 staged in E[j][lane]; returns the packet total S_{P-1}.
+// bits [POS, POS + 32) of the 512-bit packet held in 16 words
+template <int POS>
+__device__ __forceinline__ uint32_t window32(const uint32_t (&w)[16]) {
+  constexpr int k = POS >> 5, s = POS & 31;
+  static_assert(POS >= 0 && POS + 32 <= 512, "window outside the packet");
+  if constexpr (s == 0) return w[k];
+  else return __funnelshift_r(w[k], w[k + 1], s);
+}
+
+// Per-lane decode of one packet.  Element j: 10-bit column at bit P + 10j, B-bit value at bit
+// 11P + Bj (fpga_utils.hpp:349-384).  Running prefix S_j = sum_{i<=j} val_i * q[col_i] (int32,
+// wrapping) is staged four at a time in E4[(j/4)*32 + lane]; returns S_{P-1}.
 template <int B, bool SGN>
 struct PacketDecoder {
   static constexpr int P = packet_elems(B);
+  static constexpr int NG = (P + 3) / 4;
+  using Flags = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
+
   template <int J>
-  __device__ __forceinline__ static void step(const uint32_t (&w)[16], const int32_t* qt,
-                                              uint32_t lane, uint32_t* E, int32_t& S) {
+  __device__ __forceinline__ static void step(const uint32_t (&w)[16], const char* qtb,
+                                              uint32_t lane2, uint4* E4, int32_t& S,
+                                              int32_t (&s4)[4]) {
     if constexpr (J < P) {
-      const uint32_t col = ufield<P + 10 * J, 10>(w);
-      int32_t v;
-      if constexpr (SGN) v = sfield<11 * P + B * J, B>(w);
-      else v = (int32_t)ufield<11 * P + B * J, B>(w);
-      const int32_t q = qt[(col << 5) | lane];
+      // column window starting 6 bits early: (col << 6) lands at bits 6..15, the byte offset
+      // of q[col] in the lane-replicated table qt[col][32] (int16)
+      const uint32_t y = window32<P + 10 * J - 6>(w);
+      const int32_t q = *reinterpret_cast<const int16_t*>(qtb + ((y & 0xFFC0u) | lane2));
+      const uint32_t z = window32<11 * P + B * J + B - 32>(w);  // value in the top B bits
+      const int32_t v = SGN ? ((int32_t)z >> (32 - B)) : (int32_t)(z >> (32 - B));
       S += v * q;
-      if constexpr (J < P - 1) E[J * 32 + lane] = (uint32_t)S;
-      step<J + 1>(w, qt, lane, E, S);
+      s4[J & 3] = S;
+      if constexpr ((J & 3) == 3 || J == P - 1)
+        E4[(J >> 2) * 32] = make_uint4((uint32_t)s4[0], (uint32_t)s4[1], (uint32_t)s4[2], (uint32_t)s4[3]);
+      step<J + 1>(w, qtb, lane2, E4, S, s4);
     }
   }
-  __device__ __forceinline__ static int32_t run(const uint32_t (&w)[16], const int32_t* qt,
-                                                uint32_t lane, uint32_t* E) {
+  __device__ __forceinline__ static int32_t run(const uint32_t (&w)[16], const char* qtb,
+                                                uint32_t lane2, uint4* E4) {
     int32_t S = 0;
-    step<0>(w, qt, lane, E, S);
+    int32_t s4[4] = {0, 0, 0, 0};
+    step<0>(w, qtb, lane2, E4, S, s4);
     return S;
   }
-  __device__ __forceinline__ static uint64_t flags(const uint32_t (&w)[16]) {
+  __device__ __forceinline__ static Flags flags(const uint32_t (&w)[16]) {
     if constexpr (P <= 32) {
-      return (uint64_t)(w[0] & ((P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u)));
+      return w[0] & ((P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u));
     } else {
       return (uint64_t)w[0] | ((uint64_t)(w[1] & ((1u << (P - 32)) - 1u)) << 32);
     }
   }
 };
+
+__device__ __forceinline__ int ffs_flags(uint32_t f) { return __ffs(f) - 1; }
+__device__ __forceinline__ int ffs_flags(uint64_t f) { return __ffsll((long long)f) - 1; }
+__device__ __forceinline__ int fls_flags(uint32_t f) { return 31 - __clz(f); }
+__device__ __forceinline__ int fls_flags(uint64_t f) { return 63 - __clzll((long long)f); }
+__device__ __forceinline__ uint32_t popc_flags(uint32_t f) { return __popc(f); }
+__device__ __forceinline__ uint32_t popc_flags(uint64_t f) { return __popcll(f); }
 
 __device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, uint32_t lane) {
 #pragma unroll
@@ -163,105 +203,137 @@ __device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, uint32_t lane) {
   return v;
 }
 
-// One warp streams tiles [tb, te) and owns every row whose first entry lies in them; the row
-// still open at te is finished by reading on until the next row flag.
+struct RangeState {
+  bool open_owned;  // the row open at the current position started inside the range
+  uint32_t startG;  // running sum before the open row's first entry
+  uint32_t carryG;  // running sum before the current tile
+};
+
+// S_{j-1} of this lane's packet (0 for j == 0)
+__device__ __forceinline__ uint32_t prefix_before(const uint32_t* Ew, uint32_t lane, int j) {
+  if (j == 0) return 0u;
+  const int i = j - 1;
+  return Ew[(((i >> 2) * 32 + lane) << 2) | (i & 3)];
+}
+
+// One tile of a warp's range.  Returns true once the range is complete.
 template <int B, bool SGN, int MODE>
-__device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te, uint32_t sample_tile,
-                           const int32_t* qt, uint32_t* E) {
+__device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32_t te,
+                                          const uint32_t (&w)[16], uint32_t rowbase,
+                                          RangeState& st, const Emitter<MODE>& emit,
+                                          const char* qtb, uint4* E4) {
   using D = PacketDecoder<B, SGN>;
-  constexpr int P = D::P;
+  using Flags = typename D::Flags;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (t >= a.n_tiles) {  // the end of the matrix closes the last row
+    if (st.open_owned && lane == 0) emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG));
+    return true;
+  }
+  const uint32_t* Ew = reinterpret_cast<const uint32_t*>(E4);  // warp's staging area
+  const Flags F = D::flags(w);
+  const int32_t total = D::run(w, qtb, lane << 1, E4 + lane);
+  const uint32_t incl = warp_incl_sum((uint32_t)total, lane);
+  const uint32_t LB = st.carryG + incl - (uint32_t)total;  // running sum before this packet
+  const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
+  if (t >= te) {  // closing: only the first flag from here on matters
+    if (has_mask == 0) {
+      st.carryG += tileSum;
+      return false;
+    }
+    if (lane == (uint32_t)(__ffs(has_mask) - 1)) {
+      const uint32_t Gb = LB + prefix_before(Ew, lane, ffs_flags(F));
+      if (st.open_owned) emit(rowbase, (int32_t)(Gb - st.startG));
+    }
+    return true;
+  }
+  const uint32_t nf = popc_flags(F);
+  const uint32_t rbase = rowbase + warp_incl_sum(nf, lane) - nf;
+  uint32_t lastGb = 0;
+  if (F) lastGb = LB + prefix_before(Ew, lane, fls_flags(F));
+  const uint32_t left = has_mask & ((1u << lane) - 1u);
+  const uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, left ? (31 - __clz(left)) : 0u);
+  uint32_t prevG = left ? inhG : st.startG;
+  Flags f = F;
+  uint32_t row = rbase;
+  if (f && !left && !st.open_owned) {  // first flag closes a row started before the range
+    prevG = LB + prefix_before(Ew, lane, ffs_flags(f));
+    f &= f - 1;
+    row++;
+  }
+  while (f) {  // each flag closes the row before it
+    const int j = ffs_flags(f);
+    f &= f - 1;
+    const uint32_t Gb = LB + prefix_before(Ew, lane, j);
+    emit(row, (int32_t)(Gb - prevG));
+    prevG = Gb;
+    row++;
+  }
+  if (has_mask) {
+    st.startG = __shfl_sync(0xFFFFFFFFu, lastGb, 31 - __clz(has_mask));
+    st.open_owned = true;
+  }
+  st.carryG += tileSum;
+  return false;
+}
+
+// One warp streams tiles [tb, te) and owns every row whose first entry lies in them; the row
+// still open at te is finished by reading on until the next row flag.  Tiles are prefetched
+// three deep in registers.
+template <int B, bool SGN, int MODE>
+__device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
+                           const Emitter<MODE>& emit, const char* qtb, uint4* E4) {
   const uint32_t lane = threadIdx.x & 31u;
   if (tb >= te) return;
-  bool open_owned = (tb == 0);  // row 0 starts at entry 0 without a flag
-  uint32_t startG = 0;          // running sum before the open row's first entry
-  uint32_t carryG = 0;          // running sum before the current tile
-  uint32_t w[16], nw[16];
-  load_tile(a.tiles, tb, lane, w);
-  for (uint32_t t = tb;; t++) {
-    if (t >= a.n_tiles) {  // end of the matrix closes the last row
-      if (open_owned && lane == 0) emit_row<MODE>(a, a.n_rows - 1, (int32_t)(carryG - startG), sample_tile);
-      return;
+  RangeState st{tb == 0, 0u, 0u};  // row 0 starts at entry 0 without a flag
+  uint32_t wa[16], wb[16];
+  uint32_t ra = 0, rb = 0;
+  auto fetch = [&](uint32_t t, uint32_t (&w)[16], uint32_t& r) {
+    if (t < a.n_tiles) {
+      load_tile(a.tiles, t, lane, w);
+      r = __ldg(a.tile_rowbase + t);
     }
-    const bool closing = (t >= te);
-    if (t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
-    const uint64_t F = D::flags(w);
-    const int32_t total = D::run(w, qt, lane, E);
-    __syncwarp();
-    const uint32_t incl = warp_incl_sum((uint32_t)total, lane);
-    const uint32_t LB = carryG + incl - (uint32_t)total;  // running sum before this packet
-    const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
-    if (closing) {
-      if (has_mask == 0) {  // the open row spans this whole tile
-        carryG += tileSum;
-#pragma unroll
-        for (int i = 0; i < 16; i++) w[i] = nw[i];
-        continue;
-      }
-      const uint32_t l0 = __ffs(has_mask) - 1;
-      if (lane == l0) {
-        const int j0 = __ffsll((long long)F) - 1;
-        const uint32_t Gb = LB + (j0 ? E[(j0 - 1) * 32 + lane] : 0u);
-        if (open_owned) {
-          const uint32_t fl = __ldg(a.tile_rowbase + t) + 0u;
-          // rows completed before lane l0 in this tile: none (l0 is the first lane with a flag)
-          emit_row<MODE>(a, fl, (int32_t)(Gb - startG), sample_tile);
-        }
-      }
-      return;
-    }
-    // flags before this lane -> row ids
-    const uint32_t nf = (uint32_t)__popcll(F);
-    const uint32_t nf_incl = warp_incl_sum(nf, lane);
-    const uint32_t rbase = __ldg(a.tile_rowbase + t) + nf_incl - nf;
-    // G before the last flag of each lane, inherited by lanes to its right
-    uint32_t lastGb = 0;
-    if (F) {
-      const int jl = 63 - __clzll((long long)F);
-      lastGb = LB + (jl ? E[(jl - 1) * 32 + lane] : 0u);
-    }
-    const uint32_t left = has_mask & ((1u << lane) - 1u);
-    uint32_t src = left ? (31 - __clz(left)) : 0u;
-    uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, src);
-    uint32_t prevG = left ? inhG : startG;
-    bool owned = left ? true : open_owned;
-    // completed rows: the k-th flag of this lane closes row rbase + k
-    uint64_t f = F;
-    uint32_t k = 0;
-    while (f) {
-      const int j = __ffsll((long long)f) - 1;
-      f &= f - 1;
-      const uint32_t Gb = LB + (j ? E[(j - 1) * 32 + lane] : 0u);
-      if (owned) emit_row<MODE>(a, rbase + k, (int32_t)(Gb - prevG), sample_tile);
-      prevG = Gb;
-      owned = true;
-      k++;
-    }
-    if (has_mask) {
-      const uint32_t lhi = 31 - __clz(has_mask);
-      startG = __shfl_sync(0xFFFFFFFFu, lastGb, lhi);
-      open_owned = true;
-    }
-    carryG += tileSum;
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < 16; i++) w[i] = nw[i];
+  };
+  fetch(tb, wa, ra);
+  for (uint32_t t = tb;; t += 2) {
+    fetch(t + 1, wb, rb);
+    if (tile_step<B, SGN, MODE>(a, t, te, wa, ra, st, emit, qtb, E4)) return;
+    fetch(t + 2, wa, ra);
+    if (tile_step<B, SGN, MODE>(a, t + 1, te, wb, rb, st, emit, qtb, E4)) return;
   }
+}
+
+template <int B>
+__host__ __device__ constexpr size_t plain_stage_bytes() {
+  return (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;  // per warp
 }
 
 template <int B, bool SGN, int MODE>
 __global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int P = packet_elems(B);
-  int32_t* qt = reinterpret_cast<int32_t*>(smem);                 // [cols][32]
-  uint32_t* Eall = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * 128);
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  uint32_t* E = Eall + warp * (P - 1) * 32;
-  // replicate the query once per lane so that lane l always reads bank l
+  const uint32_t warp = threadIdx.x >> 5;
+  const char* qtb = reinterpret_cast<const char*>(smem);            // int16 qt[cols][32]
+  int16_t* qt = reinterpret_cast<int16_t*>(smem);
+  uint4* E4all = reinterpret_cast<uint4*>(smem + (size_t)a.cols * 64);
+  uint4* E4 = E4all + (size_t)warp * (plain_stage_bytes<B>() / 16);
+  uint32_t* thr_s = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * 64 +
+                                                kWarpsPlain * plain_stage_bytes<B>());
+  // replicate the query once per lane (lanes 2m and 2m+1 share bank m + 16 * (col & 1), so a
+  // gather costs at most two wavefronts); the bytes are
+  // staged through the (not yet used) prefix area so the fill needs one global round trip
+  int8_t* qstage = reinterpret_cast<int8_t*>(E4all);
+  for (uint32_t i = threadIdx.x; i < a.cols; i += blockDim.x) qstage[i] = a.q8[i];
+  __syncthreads();
   for (uint32_t i = threadIdx.x; i < a.cols * 32u; i += blockDim.x) {
     const uint32_t c = i >> 5;
-    int32_t v = SGN ? (int32_t)a.q8[c] : (int32_t)(uint8_t)a.q8[c];
-    qt[i] = v;
+    qt[i] = SGN ? (int16_t)qstage[c] : (int16_t)(uint8_t)qstage[c];
+  }
+  __syncthreads();
+  uint32_t thr0 = 0;
+  if constexpr (MODE == MODE_FILTER) {
+    if (a.split > 1 && a.split <= kThrSmemMax)
+      for (uint32_t i = threadIdx.x; i < a.split; i += blockDim.x) thr_s[i] = a.thr[i];
+    thr0 = a.thr[0];
   }
   __syncthreads();
   const uint32_t gw = blockIdx.x * kWarpsPlain + warp;
@@ -269,14 +341,15 @@ __global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
   if constexpr (MODE == MODE_SAMPLE) {
     for (uint32_t s = gw; s < a.n_sample_tiles; s += nw) {
       const uint32_t t = s * a.sample_stride;
-      cand_range<B, SGN, MODE>(a, t, t + 1, s, qt, E);
+      Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s)};
+      cand_range<B, SGN, MODE>(a, t, t + 1, em, qtb, E4);
     }
   } else {
     const uint64_t n = a.n_tiles;
     const uint32_t tb = (uint32_t)((n * gw) / nw), te = (uint32_t)((n * (gw + 1)) / nw);
-    cand_range<B, SGN, MODE>(a, tb, te, 0, qt, E);
+    Emitter<MODE> em{a, thr_s, thr0, 0u};
+    cand_range<B, SGN, MODE>(a, tb, te, em, qtb, E4);
   }
-  (void)lane;
 }
 
 }  // namespace dev
@@ -399,7 +472,10 @@ __device__ __forceinline__ void warp_find_suffix_bin(const uint32_t* hist, int n
 // >= L with overwhelming probability; a miss is detected later (ST_MISS) and repaired.
 // Also resets the partition's survivor counter.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_threshold(const uint32_t* __restrict__ keys, uint32_t ld_keys,
+// Sample keys of query q: keys[base(q) + i * stride] with base(q) = q * ld_keys and stride 1
+// (one query per pass), or, when qblk > 0 (batched passes of qblk queries),
+// base(q) = (q / qblk) * qblk * ld_keys + q % qblk and stride qblk.
+__global__ void k_threshold(const uint32_t* __restrict__ keys_all, uint32_t ld_keys, uint32_t qblk,
                             const uint32_t* __restrict__ part_begin, uint32_t split,
                             const uint32_t* __restrict__ r_part, uint32_t* __restrict__ thr,
                             uint32_t* __restrict__ cnt) {
@@ -408,7 +484,14 @@ __global__ void k_threshold(const uint32_t* __restrict__ keys, uint32_t ld_keys,
   __shared__ int s_bin;
   __shared__ uint32_t s_above;
   const uint32_t p = blockIdx.x, q = blockIdx.y;
-  const uint32_t* kk = keys + (size_t)q * ld_keys;
+  const uint32_t stride = qblk ? qblk : 1u;
+  const uint32_t* kb = keys_all + (qblk ? (size_t)(q / qblk) * qblk * ld_keys + q % qblk
+                                        : (size_t)q * ld_keys);
+  struct Strided {
+    const uint32_t* b;
+    uint32_t s;
+    __device__ __forceinline__ uint32_t operator[](uint32_t i) const { return b[(size_t)i * s]; }
+  } kk{kb, stride};
   const uint32_t a = part_begin[p], b = part_begin[p + 1];
   const uint32_t n = b - a;
   const uint32_t r = r_part[p];
@@ -454,8 +537,15 @@ __global__ void k_threshold(const uint32_t* __restrict__ keys, uint32_t ld_keys,
   const int sh1 = bl > 11 ? bl - 11 : 0;
   for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  for (uint32_t i = a + threadIdx.x; i < b; i += blockDim.x)
-    atomicAdd(&hist[(kk[i] - mn) >> sh1], 1u);
+  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x) {
+    const uint32_t i = i0 + threadIdx.x;
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, i < b);
+    if (i < b) {
+      const uint32_t bin = (kk[i] - mn) >> sh1;
+      const unsigned peers = __match_any_sync(act, bin);
+      if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+    }
+  }
   __syncthreads();
   if (threadIdx.x < 32) warp_find_suffix_bin(hist, kHistBins, r, &s_bin, &s_above);
   __syncthreads();
@@ -468,9 +558,15 @@ __global__ void k_threshold(const uint32_t* __restrict__ keys, uint32_t ld_keys,
   __syncthreads();
   for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  for (uint32_t i = a + threadIdx.x; i < b; i += blockDim.x) {
-    uint32_t d = kk[i] - mn;
-    if ((d >> sh1) == b1) atomicAdd(&hist[(d >> sh2) & ((1u << (sh1 - sh2)) - 1u)], 1u);
+  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x) {
+    const uint32_t i = i0 + threadIdx.x;
+    const bool in = (i < b) && (((kk[i] - mn) >> sh1) == b1);
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, in);
+    if (in) {
+      const uint32_t bin = ((kk[i] - mn) >> sh2) & ((1u << (sh1 - sh2)) - 1u);
+      const unsigned peers = __match_any_sync(act, bin);
+      if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+    }
   }
   __syncthreads();
   if (threadIdx.x < 32) warp_find_suffix_bin(hist, kHistBins, r - above1, &s_bin, &s_above);

@@ -151,7 +151,9 @@ def main():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--batch", type=int, default=64, help="queries per step")
+    ap.add_argument("--batch", type=int, default=64, help="queries per plain step")
+    ap.add_argument("--batch-batched", type=int, default=256, help="queries per batched step")
+    ap.add_argument("--steps-batched", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-queries", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
@@ -160,6 +162,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
+    args.steps_batched = max(1, args.steps_batched)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -179,66 +182,82 @@ def main():
 
     rows = args.rows
     ptr, col, val = make_matrix(rows)
-    B = args.batch
-    eng = E.SpMV(rows, COLS, ptr=ptr, col=col, val=val, bits=BITS, quant=E.QUANT_SYM_GLOBAL,
-                 split=1, ck=CK, k_max=K, max_batch=B, device=local, flags=E.FLAG_PROFILE)
-    info = eng.info()
-    npool = B * 4
-    Qh = make_queries(npool, seed=SEED + 1 + rank)
-    dq = torch.from_numpy(Qh).cuda()
-    di = torch.empty((B, K), dtype=torch.int32, device="cuda")
-    ds = torch.empty((B, K), dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()  # the engine's kernels and the timing events share it
     sptr = stream.cuda_stream
-    torch.cuda.synchronize()
 
-    def step(s):
-        b = (s % 4) * B
-        eng.run_device(dq[b:b + B].data_ptr(), B, K, di.data_ptr(), ds.data_ptr(), sptr)
+    def measure(eng, B, steps, warmup, tag):
+        """Device-timed steps of B resident queries; returns (ms, stats, repaired, clocks)."""
+        npool = B * 4
+        Qh = make_queries(npool, seed=SEED + 1 + rank)
+        dq = torch.from_numpy(Qh).cuda()
+        di = torch.empty((B, K), dtype=torch.int32, device="cuda")
+        ds = torch.empty((B, K), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
 
-    for s in range(args.warmup):
-        step(s)
-    torch.cuda.synchronize()
-    eng.finish()
-    eng.stats(reset=True)
+        def step(s):
+            b = (s % 4) * B
+            eng.run_device(dq[b:b + B].data_ptr(), B, K, di.data_ptr(), ds.data_ptr(), sptr)
 
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for s in range(args.steps):
-        step(s)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    clk = clocks.stop()
-    repaired = eng.finish()
-    st = eng.stats(reset=True)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    qps = world * args.steps * B / (ms / 1e3)
+        for s in range(warmup):
+            step(s)
+        torch.cuda.synchronize()
+        eng.finish()
+        eng.stats(reset=True)
+        clocks = ClockSampler(local)
+        clocks.start()
+        time.sleep(0.3)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(steps):
+            step(s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        clk = clocks.stop()
+        repaired = eng.finish()
+        st = eng.stats(reset=True)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, st, repaired, clk, Qh
 
-    # dominant kernel: the full-matrix candidate pass; algorithmic bytes per launch = the
-    # Ultra-CSR packets + the tile row bases + the int8 query
-    alg_bytes = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS
+    common = dict(bits=BITS, quant=E.QUANT_SYM_GLOBAL, split=1, ck=CK, k_max=K, device=local,
+                  flags=E.FLAG_PROFILE)
+    # plain: one candidate pass per query
+    Bp = args.batch
+    eng_p = E.SpMV(rows, COLS, ptr=ptr, col=col, val=val, max_batch=Bp, batch_tile=1, **common)
+    info = eng_p.info()
+    ms_p, st_p, rep_p, clk_p, _ = measure(eng_p, Bp, args.steps, args.warmup, "plain")
+    plain_qps = world * args.steps * Bp / (ms_p / 1e3)
+    plain_launch_ms = st_p["cand_ms"] / max(st_p["cand_timed"], 1)
+    eng_p.close()
+    # batched: one candidate pass per 128 queries
+    Bb = args.batch_batched
+    eng = E.SpMV(rows, COLS, ptr=ptr, col=col, val=val, max_batch=Bb, batch_tile=128, **common)
+    ms, st, repaired, clk, Qh = measure(eng, Bb, args.steps_batched, args.warmup, "batched")
+    B = Bb
+    qps = world * args.steps_batched * Bb / (ms / 1e3)
+
+    # dominant kernel of the batched path: the batched candidate pass; algorithmic bytes per
+    # launch = Ultra-CSR packets + tile row bases + the 128-query table
+    alg_bytes = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS * 128
     cand_ms = st["cand_ms"] / max(st["cand_timed"], 1)
     achieved = alg_bytes / (cand_ms / 1e3) / 1e9
+    plain_alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS
+    plain_achieved = plain_alg / (plain_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic("cand_pass_10Mx1024_b8.md")
+    traffic = profile_traffic("cand_batch_10Mx1024_b8.md")
+    plain_traffic = profile_traffic("cand_pass_10Mx1024_b8.md")
 
-    # end to end through the host-buffer C ABI
-    Kk = max(3, min(args.steps, 10))
-    out_i = np.zeros((B, K), np.uint32)
-    out_s = np.zeros((B, K), np.float32)
+    # end to end through the host-buffer C ABI (batched engine)
+    Kk = max(3, min(args.steps_batched, 10))
     eng.Q_reset(Qh[:B])
     eng(k=K)
     torch.cuda.synchronize()
@@ -251,7 +270,6 @@ def main():
     e2e_qps = world * Kk * B / e2e_s
 
     # correctness of the measured configuration (outside the timed regions)
-    gi = di.cpu().numpy().view(np.uint32)
     line_extra = {}
     if rank == 0:
         import oracle as orc
@@ -278,24 +296,30 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "steps": args.steps_batched, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps_batched,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded; reference matrices not shipped)",
             "config": {"workload": f"{rows // 1_000_000}Mx1024 deg U{{10..30}} U(0,1), 8-bit Ultra-CSR, CK=1024, K=100, split=1",
                        "rows": rows, "cols": COLS, "nnz": info["nnz"], "bits": BITS, "ck": CK,
-                       "k": K, "batch": B, "path": "plain (one candidate pass per query)",
+                       "k": K, "batch": Bb, "path": "batched (one candidate pass per 128 queries)",
+                       "plain_batch": Bp, "plain_steps": args.steps,
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (492 MB packets per pass)"},
-            "plain_qps": qps, "batched_qps": None,
-            "hbm_gbs_candidate_pass": achieved,
+            "batched_qps": qps, "plain_qps": plain_qps, "batched_over_plain": qps / plain_qps,
+            "hbm_gbs_batched_pass": achieved, "hbm_gbs_plain_pass": plain_achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_cand_plain<8,signed,FILTER>",
+                         "kernel": "k_cand_batch<8,signed,FILTER> (128 queries per pass)",
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": cand_ms},
+            "plain_roofline": {"bound": "hbm", "achieved": plain_achieved, "peak": peak,
+                               "unit": "GB/s", "frac": plain_achieved / peak,
+                               "traffic": plain_traffic, "kernel": "k_cand_plain<8,signed,FILTER>",
+                               "alg_bytes_per_launch": plain_alg, "launch_ms": plain_launch_ms},
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": B * COLS * 4,
                     "d2h_bytes_per_step": B * K * 8},
-            "gpu_launches": st["launches"], "repaired_queries": repaired + st["repaired"],
-            "clocks": clk,
+            "gpu_launches": st["launches"], "repaired_queries": repaired + st["repaired"] + rep_p + st_p["repaired"],
+            "clocks": clk, "clocks_plain": clk_p,
         }
         line.update(line_extra)
         print(json.dumps(line), flush=True)

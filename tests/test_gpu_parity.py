@@ -185,3 +185,51 @@ def test_reference_api_shape():
     assert all(keys[i] ^ 0x80000000 == (s & 0xFFFFFFFF) for i, s in zip(idx, res))
     order = list(zip(res, idx))
     assert order == sorted(order, reverse=True)
+
+
+# ---- batched candidate pass (one matrix read per tile of up to 128 queries) -------------------
+
+@pytest.mark.parametrize("bits,quant,split,ck,nq", [(8, 0, 1, 1024, 128), (6, 0, 32, 512, 37),
+                                                   (4, 1, 1, 256, 200), (8, 2, 8, 512, 64),
+                                                   (4, 0, 32, 1024, 130)])
+def test_batched_matches_oracle(bits, quant, split, ck, nq):
+    rows, cols, k = 20000, 1024, 100
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 17 + bits, bits, quant, split, ck, k,
+                  nq=nq, batch_tile=128)
+    assert eng.info()["batch_tile"] == 128
+    Q = queries(cols, nq, 11, signed=(quant == 0))
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    for i in range(0, nq, max(1, nq // 9)):
+        oi, os_, cand = m.two_stage(Q[i], split, ck, k)
+        n = len(oi)
+        assert np.array_equal(idx[i, :n], oi), i
+        assert np.array_equal(sc[i, :n], os_), i
+        gi, _, _ = eng.read_candidates(i)
+        keys = m.keys(Q[i])
+        exp = cand[np.lexsort((-cand.astype(np.int64), -keys[cand].astype(np.int64)))]
+        assert np.array_equal(gi, exp), i
+
+
+def test_batched_equals_plain_and_long_rows():
+    rows, cols = 6000, 700
+    ptr, col, val = E.gen_matrix(E.GEN_GAMMA_DEG, rows, cols, 120, 700, seed=77)
+    Q = queries(cols, 40, 3, signed=True)
+    out = []
+    for bt in (1, 128):
+        eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=6, split=4, ck=256, k_max=50,
+                     max_batch=40, batch_tile=bt)
+        eng.Q_reset(Q)
+        eng(k=50)
+        out.append(eng.read_topk())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_batched_tiny_and_zero_queries():
+    rows, cols = 70, 96
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 1, 12, 5, 8, 0, 32, 64, 10, nq=20,
+                  batch_tile=128)
+    Q = queries(cols, 20, 8, signed=True)
+    Q[3] = 0.0
+    check_run(m, eng, Q, 32, 64, 10)
