@@ -177,41 +177,41 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
     }
     __syncwarp();
     // ---- phase B: lanes = queries ------------------------------------------------------------
+#pragma unroll 2
     for (int g = 0; g < NG; g++) {
       const uint4 o4 = reinterpret_cast<const uint4*>(offs)[g];
       const uint32_t v4 = reinterpret_cast<const uint32_t*>(vals)[g];
       const uint32_t f4 = reinterpret_cast<const uint32_t*>(flg)[g];
       uint32_t W[4], V[4];
-      W[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x | lane4));
-      W[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y | lane4));
-      W[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z | lane4));
-      W[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w | lane4));
+      W[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x + lane4));
+      W[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y + lane4));
+      W[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z + lane4));
+      W[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w + lane4));
       transpose4(W, V);
       if (f4 == 0) {
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4, V[q], acc[q]);
         continue;
       }
-      // a row starts at one or more of the four elements: split the group at each flag
-      uint32_t lo = 0;  // first element of the group not yet accumulated
-      for (int i = 0; i < 4; i++) {
-        if (!((f4 >> (8 * i)) & 1u)) continue;
-        if (i > lo) {
-          const uint32_t m = (0xFFFFFFFFu >> (8 * (4 - i))) & (0xFFFFFFFFu << (8 * lo));
+      // rows start at the flagged elements: bit i of fm <=> element i of the group
+      uint32_t fm = (f4 * 0x01020408u) >> 24;
+      uint32_t lo_mask = 0xFFFFFFFFu;  // bytes of the group not yet accumulated
+      do {
+        const int i = __ffs(fm) - 1;
+        fm &= fm - 1;
+        const uint32_t m = lo_mask & ~(0xFFFFFFFFu << (8 * i));  // bytes [lo, i)
 #pragma unroll
-          for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & m, V[q], acc[q]);
-        }
+        for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & m, V[q], acc[q]);
         if (owned) rows.finish(row, acc);
         if (closing) return;
         row++;
         owned = true;
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] = 0;
-        lo = i;
-      }
-      const uint32_t m = 0xFFFFFFFFu << (8 * lo);
+        lo_mask = 0xFFFFFFFFu << (8 * i);
+      } while (fm);
 #pragma unroll
-      for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & m, V[q], acc[q]);
+      for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & lo_mask, V[q], acc[q]);
     }
     __syncwarp();
 #pragma unroll
