@@ -155,7 +155,8 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
       return;
     }
     const bool closing = (t >= te);
-    if (t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
+    // prefetch one tile ahead up to the first closing tile; later tiles are read on demand
+    if (t + 1 <= te && t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
     // ---- phase A: this lane's packet -> records ----------------------------------------------
     {
       using D = PacketDecoder<B, SGN>;
@@ -214,8 +215,12 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
       for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & lo_mask, V[q], acc[q]);
     }
     __syncwarp();
+    if (t + 1 > te) {
+      if (t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, w);
+    } else {
 #pragma unroll
-    for (int i = 0; i < 16; i++) w[i] = nw[i];
+      for (int i = 0; i < 16; i++) w[i] = nw[i];
+    }
   }
 }
 

@@ -294,12 +294,16 @@ __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
       r = __ldg(a.tile_rowbase + t);
     }
   };
+  // tiles up to te (the first closing tile) are prefetched one ahead; tiles past te are read
+  // only when the open row runs on through the closing tile
   fetch(tb, wa, ra);
   for (uint32_t t = tb;; t += 2) {
-    fetch(t + 1, wb, rb);
+    if (t + 1 <= te) fetch(t + 1, wb, rb);
     if (tile_step<B, SGN, MODE>(a, t, te, wa, ra, st, emit, qtb, E4)) return;
-    fetch(t + 2, wa, ra);
+    if (t + 1 > te) fetch(t + 1, wb, rb);
+    if (t + 2 <= te) fetch(t + 2, wa, ra);
     if (tile_step<B, SGN, MODE>(a, t + 1, te, wb, rb, st, emit, qtb, E4)) return;
+    if (t + 2 > te) fetch(t + 2, wa, ra);
   }
 }
 
