@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -953,3 +954,168 @@ int aes_read_candidates(aes_handle* h, uint32_t query, uint32_t* idx, int32_t* s
 }
 
 }  // extern "C"
+
+// =============================================================================================
+// No-allocation entry point
+// =============================================================================================
+// Per-query scratch of aes_run_noalloc lives in this fixed device array instead of memory the
+// call allocates.  The array is part of the library's device image: every GPU that loads the
+// library holds these bytes until the process exits.
+static constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};  // device address of g_noalloc_scratch, per device ordinal
+
+// Device address of the scratch array on the current device (looked up once per device; host
+// code must not use the symbol itself as an address).
+int noalloc_scratch(int dev, unsigned char** out) {
+  if (dev < 0 || dev >= 256) return aes::fail(AES_ERR_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return aes::fail(AES_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  return AES_OK;
+}
+
+struct NoAllocLayout {
+  size_t q8, skeys, thr, cnt, surv, cand, cand_key, status, total;
+};
+
+NoAllocLayout noalloc_layout(const aes::Engine& e) {
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  NoAllocLayout L{};
+  size_t o = 0;
+  L.q8 = o;       o += up(e.ld8);
+  L.skeys = o;    o += up((size_t)std::max<uint32_t>(e.n_sample_rows, 1) * 4);
+  L.thr = o;      o += up((size_t)e.split * 4);
+  L.cnt = o;      o += up((size_t)e.split * 4);
+  L.surv = o;     o += up((size_t)e.split * e.cap * 8);
+  L.cand = o;     o += up((size_t)std::max<uint32_t>(e.nslots, 1) * 4);
+  L.cand_key = o; o += up((size_t)std::max<uint32_t>(e.nslots, 1) * 4);
+  L.status = o;   o += 256;
+  L.total = o;
+  return L;
+}
+
+}  // namespace
+
+extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, uint32_t* d_idx,
+                               float* d_score, void* stream) {
+  using namespace aes::dev;
+  if (!h || !d_query || !d_idx || !d_score) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  aes::Engine& e = h->e;
+  if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
+  AES_CK(cudaSetDevice(e.device));
+  const NoAllocLayout L = noalloc_layout(e);
+  if (L.total > kNoAllocScratchBytes)
+    return aes::fail(AES_ERR_UNSUPPORTED,
+                     "aes_run_noalloc: this matrix needs " + std::to_string(L.total) +
+                         " bytes of per-query scratch, over the fixed " +
+                         std::to_string(kNoAllocScratchBytes) + "-byte limit");
+  unsigned char* base = nullptr;
+  int rc = noalloc_scratch(e.device, &base);
+  if (rc) return rc;
+  cudaStream_t s = stream ? (cudaStream_t)stream : e.stream;
+  int8_t* q8 = reinterpret_cast<int8_t*>(base + L.q8);
+  uint32_t* skeys = reinterpret_cast<uint32_t*>(base + L.skeys);
+  uint32_t* thr = reinterpret_cast<uint32_t*>(base + L.thr);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(base + L.cnt);
+  uint2* surv = reinterpret_cast<uint2*>(base + L.surv);
+  uint32_t* cand = reinterpret_cast<uint32_t*>(base + L.cand);
+  uint32_t* cand_key = reinterpret_cast<uint32_t*>(base + L.cand_key);
+  uint32_t* status = reinterpret_cast<uint32_t*>(base + L.status);
+
+  // the array keeps the previous call's contents: the status word starts at zero, the survivor
+  // counters are zeroed by k_threshold, every other region is fully written before it is read
+  AES_CK(cudaMemsetAsync(status, 0, 4, s));
+  k_quantize<<<1, 256, 0, s>>>(d_query, e.cols, e.ld32, (int)e.bits, (int)e.quant,
+                               (int)e.prm.query_quant, q8, e.ld8, status);
+  AES_CK(cudaGetLastError());
+  auto plain = [&](int mode, uint32_t* keys_out) -> int {
+    PlainArgs a{};
+    a.tiles = e.d_tiles;
+    a.tile_rowbase = e.d_tile_rowbase;
+    a.n_tiles = (uint32_t)e.tiles;
+    a.n_rows = e.rows;
+    a.cols = e.cols;
+    a.q8 = q8;
+    a.rowscale = e.d_rowscale;
+    a.split = e.split;
+    a.slice = e.slice;
+    a.thr = thr;
+    a.cnt = cnt;
+    a.surv = surv;
+    a.cap = e.cap;
+    a.keys_out = keys_out;
+    a.sample_first = e.d_sample_first;
+    a.sample_stride = e.ss;
+    a.n_sample_tiles = e.n_sample_tiles;
+    int grid = e.plain_grid;
+    if (mode == MODE_SAMPLE)
+      grid = std::min<int>(grid, (int)((e.n_sample_tiles + kWarpsPlain - 1) / kWarpsPlain));
+    grid = std::max(grid, 1);
+    aes::pick_plain((int)e.bits, e.sgn, mode)<<<grid, kThreadsPlain, e.plain_smem, s>>>(a);
+    AES_CK(cudaGetLastError());
+    return AES_OK;
+  };
+  if ((rc = plain(MODE_SAMPLE, skeys))) return rc;
+  k_threshold<<<dim3(e.split, 1), 512, 0, s>>>(skeys, e.n_sample_rows, 0, e.d_part_sample_begin,
+                                               e.split, e.d_part_r, thr, cnt);
+  AES_CK(cudaGetLastError());
+  if ((rc = plain(MODE_FILTER, nullptr))) return rc;
+  SelectArgs sa{};
+  sa.surv = surv;
+  sa.cnt = cnt;
+  sa.cap = e.cap;
+  sa.split = e.split;
+  sa.slice = e.slice;
+  sa.n_rows = e.rows;
+  sa.ntop = e.ntop;
+  sa.cand = cand;
+  sa.cand_key = cand_key;
+  sa.status = status;
+  k_select<false><<<dim3(e.split, 1), 512, 0, s>>>(sa);
+  AES_CK(cudaGetLastError());
+  FinalArgs fa{};
+  fa.csr_ptr = e.d_csr_ptr;
+  fa.csr_col = e.d_csr_col;
+  fa.csr_val = e.d_csr_val;
+  fa.q32 = d_query;
+  fa.ld32 = e.ld32;
+  fa.cols = e.cols;
+  fa.cand = cand;
+  fa.nslots = e.nslots;
+  fa.npow2 = e.npow2;
+  fa.k = k;
+  fa.out_idx = d_idx;
+  fa.out_score = d_score;
+  fa.status = status;
+  k_final<<<1, 1024, e.final_smem, s>>>(fa);
+  AES_CK(cudaGetLastError());
+  uint32_t st = 0;
+  AES_CK(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s));
+  AES_CK(cudaStreamSynchronize(s));
+  if (st & ST_QUERY) return aes::fail(AES_ERR_QUERY, "query has negative entries under an unsigned quantiser");
+  if (st & (ST_MISS | ST_OVERFLOW)) {
+    // exact slow path: every row's key into the handle's key array (reserved at creation),
+    // each partition's Top-CK from it, then the FP32 rescoring
+    if ((rc = plain(MODE_ALL, e.d_allkeys))) return rc;
+    sa.allkeys = e.d_allkeys;
+    sa.q0 = 0;
+    k_select<true><<<dim3(e.split, 1), 512, 0, s>>>(sa);
+    AES_CK(cudaGetLastError());
+    fa.status = nullptr;
+    k_final<<<1, 1024, e.final_smem, s>>>(fa);
+    AES_CK(cudaGetLastError());
+    AES_CK(cudaStreamSynchronize(s));
+  }
+  return AES_OK;
+}

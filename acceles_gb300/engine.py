@@ -40,7 +40,7 @@ GEN_FIXED_UNIFORM = 3
 
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
            "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
-           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats"]
+           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc"]
 
 FLAG_PROFILE = 1
 
@@ -137,6 +137,9 @@ def load(build_if_missing: bool = True):
     L.aes_pack_host.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.POINTER(Params), ctypes.c_void_p, ctypes.c_uint64, _u64p,
                                 _u32p]
+    L.aes_run_noalloc.restype = ctypes.c_int
+    L.aes_run_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.aes_get_stats.restype = ctypes.c_int
     L.aes_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats), ctypes.c_int]
     L.aes_score_all.restype = ctypes.c_int
@@ -274,6 +277,12 @@ class SpMV:
         _check(load().aes_run_device(self._h, ctypes.c_void_p(d_queries), nq, k,
                                      ctypes.c_void_p(d_idx), ctypes.c_void_p(d_score),
                                      ctypes.c_void_p(stream) if stream else None))
+
+    def run_noalloc(self, d_query: int, k: int, d_idx: int, d_score: int, stream: int = 0):
+        """One device-resident query through the path without allocating (see acceles.h)."""
+        _check(load().aes_run_noalloc(self._h, ctypes.c_void_p(d_query), k,
+                                      ctypes.c_void_p(d_idx), ctypes.c_void_p(d_score),
+                                      ctypes.c_void_p(stream) if stream else None))
 
     def finish(self) -> int:
         n = ctypes.c_uint32(0)

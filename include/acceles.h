@@ -130,6 +130,19 @@ int aes_read_candidates(aes_handle* h, uint32_t query, uint32_t* idx, int32_t* s
  * buffers); it is the resident-input entry a serving loop uses. */
 int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t k,
                    uint32_t* d_idx, float* d_score, void* stream);
+/* One query through the whole path without allocating any memory.  No counterpart in the
+ * reference.  For callers that must not call cudaMalloc (or anything that allocates) once they
+ * are serving: allocation can block and synchronise the device, fail when a framework's caching
+ * allocator already holds the free memory, or is simply forbidden on a latency-critical path.
+ * The per-query scratch (quantised query, sample keys, thresholds, survivors, candidates) is a
+ * fixed 16 MiB device array inside the library instead; matrices whose scratch would not fit
+ * are rejected with AES_ERR_UNSUPPORTED.  d_query [cols] FP32, d_idx / d_score [k] are device
+ * pointers; `stream` a cudaStream_t (NULL = the handle's stream).  Synchronous.  The first call
+ * on a device looks up the array's device address, so make that call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU race and must not be issued. */
+int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, uint32_t* d_idx,
+                    float* d_score, void* stream);
+
 /* Wait for the last aes_run_device and repair any query whose fast path reported a sample
  * threshold miss or a survivor-buffer overflow (exact slow path).  *repaired (may be NULL)
  * receives the number of repaired queries. */
