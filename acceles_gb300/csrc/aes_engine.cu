@@ -118,6 +118,8 @@ struct Engine {
   uint32_t* d_out_idx = nullptr;
   float* d_out_score = nullptr;
   uint32_t* d_allkeys = nullptr;
+  uint32_t* d_exact_cand = nullptr;  // [k_max] candidates of the FP32-only pass
+  uint32_t* d_exact_key = nullptr;
 
   float* h_q32 = nullptr;         // pinned staging of queries
   uint32_t* h_status = nullptr;   // pinned
@@ -357,6 +359,8 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_allkeys, rows);
   AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 32);
+  AES_AL(d_exact_cand, std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_exact_key, std::max<uint32_t>(p.k_max, 1));
 #undef AES_AL
   AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
   AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
@@ -412,7 +416,11 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
         &occb, (const void*)pick_batch((int)bits, sgn, MODE_FILTER), batch_warps_n * 32, batch_smem));
     batch_grid = std::max(1, occb) * sm_count;
   }
-  final_smem = ((cols * 4 + 15) & ~15u) + (size_t)npow2 * 8;
+  {
+    uint32_t kp = 1;
+    while (kp < p.k_max) kp <<= 1;
+    final_smem = ((cols * 4 + 15) & ~15u) + (size_t)std::max(npow2, kp) * 8;
+  }
   AES_CK(cudaFuncSetAttribute((const void*)k_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)final_smem));
   AES_CK(cudaDeviceSynchronize());
@@ -893,6 +901,62 @@ int aes_get_stats(aes_handle* h, aes_stats* st, int reset) {
     e.n_launch = e.n_cand = e.n_repaired = e.prof_n = 0;
     e.prof_ms = 0.0;
   }
+  return AES_OK;
+}
+
+int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint64_t* ns) {
+  using namespace aes::dev;
+  if (!h || !out_idx || !out_score) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  if (!e.nq_loaded) return aes::fail(AES_ERR_STATE, "aes_set_query must come first");
+  if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
+  AES_CK(cudaSetDevice(e.device));
+  uint32_t kp = 1;
+  while (kp < k) kp <<= 1;
+  float total_ms = 0.0f;
+  for (uint32_t q = 0; q < e.nq_loaded; q++) {
+    AES_CK(cudaEventRecord(e.ev0, e.stream));
+    k_exact_all<<<e.sm_count * 8, 256, e.cols * 4, e.stream>>>(
+        e.d_csr_ptr, e.d_csr_col, e.d_csr_val, e.d_q32 + (size_t)q * e.ld32, e.cols, e.rows,
+        e.d_allkeys);
+    AES_CK(cudaGetLastError());
+    SelectArgs sa{};
+    sa.allkeys = e.d_allkeys;
+    sa.q0 = 0;
+    sa.split = 1;
+    sa.slice = e.rows;
+    sa.n_rows = e.rows;
+    sa.ntop = k;
+    sa.cand = e.d_exact_cand;
+    sa.cand_key = e.d_exact_key;
+    sa.status = e.d_status;
+    k_select<true><<<dim3(1, 1), 512, 0, e.stream>>>(sa);
+    AES_CK(cudaGetLastError());
+    FinalArgs fa{};
+    fa.csr_ptr = e.d_csr_ptr;
+    fa.csr_col = e.d_csr_col;
+    fa.csr_val = e.d_csr_val;
+    fa.q32 = e.d_q32 + (size_t)q * e.ld32;
+    fa.ld32 = e.ld32;
+    fa.cols = e.cols;
+    fa.cand = e.d_exact_cand;
+    fa.nslots = k;
+    fa.npow2 = kp;
+    fa.k = k;
+    fa.out_idx = e.d_out_idx;
+    fa.out_score = e.d_out_score;
+    fa.status = nullptr;
+    k_final<<<1, 1024, e.final_smem, e.stream>>>(fa);
+    AES_CK(cudaGetLastError());
+    AES_CK(cudaEventRecord(e.ev1, e.stream));
+    AES_CK(cudaMemcpyAsync(out_idx + (size_t)q * k, e.d_out_idx, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
+    AES_CK(cudaMemcpyAsync(out_score + (size_t)q * k, e.d_out_score, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
+    AES_CK(cudaStreamSynchronize(e.stream));
+    float ms = 0.0f;
+    AES_CK(cudaEventElapsedTime(&ms, e.ev0, e.ev1));
+    total_ms += ms;
+  }
+  if (ns) *ns = (uint64_t)((double)total_ms * 1e6);
   return AES_OK;
 }
 

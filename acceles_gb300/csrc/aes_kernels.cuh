@@ -824,3 +824,35 @@ __global__ void __launch_bounds__(1024) k_final(FinalArgs a) {
 
 }  // namespace dev
 }  // namespace aes
+
+namespace aes {
+namespace dev {
+
+// FP32 score of every row (sequential over the row's entries in column order, separately
+// rounded multiply and add: spmv_coo_gold_top_k, gold_algorithms.hpp:189-247 with V = float)
+// written as order-preserving keys.  Thread per row; the query is staged in shared memory.
+__global__ void k_exact_all(const uint32_t* __restrict__ ptr, const uint16_t* __restrict__ col,
+                            const float* __restrict__ val, const float* __restrict__ q,
+                            uint32_t cols, uint32_t rows, uint32_t* __restrict__ keys) {
+  extern __shared__ float qs[];
+  for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) qs[j] = q[j];
+  __syncthreads();
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    uint32_t e = ptr[r];
+    const uint32_t e1 = ptr[r + 1];
+    float acc = 0.0f;
+    for (; e + 4 <= e1; e += 4) {
+      const uint16_t c0 = col[e], c1 = col[e + 1], c2 = col[e + 2], c3 = col[e + 3];
+      const float v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
+      acc = __fadd_rn(acc, __fmul_rn(v0, qs[c0]));
+      acc = __fadd_rn(acc, __fmul_rn(v1, qs[c1]));
+      acc = __fadd_rn(acc, __fmul_rn(v2, qs[c2]));
+      acc = __fadd_rn(acc, __fmul_rn(v3, qs[c3]));
+    }
+    for (; e < e1; e++) acc = __fadd_rn(acc, __fmul_rn(val[e], qs[col[e]]));
+    keys[r] = key_f32(acc);
+  }
+}
+
+}  // namespace dev
+}  // namespace aes

@@ -40,7 +40,7 @@ GEN_FIXED_UNIFORM = 3
 
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
            "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
-           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc"]
+           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact"]
 
 FLAG_PROFILE = 1
 
@@ -140,6 +140,8 @@ def load(build_if_missing: bool = True):
     L.aes_run_noalloc.restype = ctypes.c_int
     L.aes_run_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.aes_run_exact.restype = ctypes.c_int
+    L.aes_run_exact.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _u32p, _f32p, _u64p]
     L.aes_get_stats.restype = ctypes.c_int
     L.aes_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats), ctypes.c_int]
     L.aes_score_all.restype = ctypes.c_int
@@ -249,6 +251,15 @@ class SpMV:
                               ctypes.byref(ns)))
         self._k = k
         return int(ns.value)
+
+    def run_exact(self, k=None):
+        """FP32-only Top-K of the loaded queries (no low-bit stage); returns (rows, scores, ns)."""
+        k = int(k or self.params.k_max)
+        idx = np.zeros((self._nq, k), np.uint32)
+        sc = np.zeros((self._nq, k), np.float32)
+        ns = ctypes.c_uint64(0)
+        _check(load().aes_run_exact(self._h, k, _p(idx, _u32p), _p(sc, _f32p), ctypes.byref(ns)))
+        return idx, sc, int(ns.value)
 
     def Q_read_result(self, res, idx, debug=0, query=0):
         """Append the candidates of `query`, sorted by (score desc, row desc)

@@ -116,6 +116,13 @@ int aes_set_query(aes_handle* h, const float* q, uint32_t nq);
  * merge of Q_read_result (:691-748). */
 int aes_run(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint64_t* ns);
 
+/* FP32-only single-stage Top-K of the loaded queries: the FP32 score of every row, sequential
+ * in column order, and the exact Top-K in sort_tuples order; no quantisation, no candidates.
+ * Replaces the software check of the reference (sw_test: spmv_coo_gold_top_k + sort_tuples,
+ * host_spmv_ucsr.cpp:841-869; gold_algorithms.hpp:189-247).  Host outputs [nq][k]; *ns gets
+ * the summed device time. */
+int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint64_t* ns);
+
 /* Candidates of query `query` of the last run in sort_tuples order (key descending, row
  * descending).  score_i32 gets the integer candidate score, key_f32 the ranking key (the
  * integer score, or rowscale * score under AES_QUANT_UNSIGNED_ROW); either may be NULL.

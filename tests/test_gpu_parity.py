@@ -233,3 +233,17 @@ def test_batched_tiny_and_zero_queries():
     Q = queries(cols, 20, 8, signed=True)
     Q[3] = 0.0
     check_run(m, eng, Q, 32, 64, 10)
+
+
+def test_fp32_only_exact_path():
+    """aes_run_exact: FP32 score of every row + Top-K equals the FP32 oracle (sw_test path)."""
+    rows, cols, k = 30000, 1024, 100
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 51, 8, 0, 1, 256, k, nq=2)
+    Q = queries(cols, 2, 52, signed=True)
+    eng.Q_reset(Q)
+    idx, sc, ns = eng.run_exact(k=k)
+    allrows = np.arange(rows, dtype=np.uint32)
+    for i in range(2):
+        s = orc.rescore_f32(m.ptr, m.col, m.val, Q[i], allrows)
+        ri, rs = orc.sort_tuples_f32(allrows, s)
+        assert np.array_equal(idx[i], ri[:k]) and np.array_equal(sc[i], rs[:k])
