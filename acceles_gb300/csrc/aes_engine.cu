@@ -12,7 +12,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -132,6 +134,21 @@ struct Engine {
   cudaStream_t last_stream = nullptr;
   bool ran = false;
 
+  // CUDA graphs of the per-batch launch sequence, keyed by its arguments
+  struct GraphKey {
+    const float* q;
+    uint32_t nq, k;
+    uint32_t* idx;
+    float* score;
+    cudaStream_t s;
+    bool operator<(const GraphKey& o) const {
+      return std::tie(q, nq, k, idx, score, s) < std::tie(o.q, o.nq, o.k, o.idx, o.score, o.s);
+    }
+  };
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  uint64_t n_graph_launch = 0;
+  uint64_t graph_launches = 0, graph_cands = 0;  // kernels inside the last captured graph
+
   // profiling / counters
   uint64_t n_launch = 0, n_cand = 0, n_repaired = 0;
   std::vector<cudaEvent_t> prof_ev;  // pairs
@@ -156,6 +173,8 @@ struct Engine {
     if (device >= 0) cudaSetDevice(device);
     for (cudaEvent_t ev : prof_ev) cudaEventDestroy(ev);
     prof_ev.clear();
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
     if (h_q32) cudaFreeHost(h_q32);
@@ -187,6 +206,8 @@ struct Engine {
   int build(const HostCSR& m, const aes_params& p);
   int enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
               cudaStream_t s);
+  int enqueue_graph(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
+                    cudaStream_t s);
   int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s);
@@ -392,10 +413,15 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     plain_smem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
                  (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
   }
+  // the shared-memory limit is an attribute of the kernel, shared by every handle: raise it to
+  // the device maximum once instead of to this handle's size
+  int smem_optin = 0;
+  AES_CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  if (plain_smem > (size_t)smem_optin) return fail(AES_ERR_UNSUPPORTED, "shared memory of the candidate pass exceeds the device limit");
   for (int mode = 0; mode < 3; mode++) {
     PlainKernel kf = pick_plain((int)bits, sgn, mode);
     AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)plain_smem));
+                                smem_optin));
   }
   int occ = 0;
   AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -409,7 +435,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     for (int mode = 0; mode < 2; mode++) {
       BatchKernel kf = pick_batch((int)bits, sgn, mode);
       AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)batch_smem));
+                                  smem_optin));
     }
     int occb = 0;
     AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -422,7 +448,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     final_smem = ((cols * 4 + 15) & ~15u) + (size_t)std::max(npow2, kp) * 8;
   }
   AES_CK(cudaFuncSetAttribute((const void*)k_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)final_smem));
+                              smem_optin));
   AES_CK(cudaDeviceSynchronize());
   return AES_OK;
 }
@@ -599,6 +625,47 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   fa.status = d_status;
   k_final<<<nq, 1024, final_smem, s>>>(fa);
   AES_CK(cudaGetLastError());
+  return AES_OK;
+}
+
+// Replays the launch sequence of enqueue() as one CUDA graph (captured on first use for these
+// arguments).  Profiling events are not recorded inside graphs.
+int Engine::enqueue_graph(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx,
+                          float* d_score, cudaStream_t s) {
+  GraphKey key{d_q, nq, k, d_idx, d_score, s};
+  auto it = graphs.find(key);
+  if (it == graphs.end()) {
+    if (graphs.size() >= 64) {
+      for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+      graphs.clear();
+    }
+    const uint32_t saved_flags = prm.flags;
+    prm.flags &= ~AES_FLAG_PROFILE;
+    const uint64_t saved_launch = n_launch, saved_cand = n_cand;
+    AES_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue(d_q, nq, k, d_idx, d_score, s);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    prm.flags = saved_flags;
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ce != cudaSuccess) return ::aes::fail(AES_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    cudaGraphExec_t ex = nullptr;
+    ce = cudaGraphInstantiate(&ex, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return ::aes::fail(AES_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+    it = graphs.emplace(key, ex).first;
+    graph_launches = n_launch - saved_launch;
+    graph_cands = n_cand - saved_cand;
+    n_launch = saved_launch;
+    n_cand = saved_cand;
+  }
+  AES_CK(cudaGraphLaunch(it->second, s));
+  n_launch += graph_launches;
+  n_cand += graph_cands;
+  n_graph_launch++;
   return AES_OK;
 }
 
@@ -828,7 +895,9 @@ int aes_run(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint
   const uint32_t nq = e.nq_loaded;
   e.last_q32 = e.d_q32;
   AES_CK(cudaEventRecord(e.ev0, e.stream));
-  int rc = e.enqueue(e.d_q32, nq, k, e.d_out_idx, e.d_out_score, e.stream);
+  int rc = (e.prm.flags & AES_FLAG_GRAPHS)
+               ? e.enqueue_graph(e.d_q32, nq, k, e.d_out_idx, e.d_out_score, e.stream)
+               : e.enqueue(e.d_q32, nq, k, e.d_out_idx, e.d_out_score, e.stream);
   if (rc) return rc;
   AES_CK(cudaEventRecord(e.ev1, e.stream));
   uint32_t rep = 0;
@@ -863,7 +932,8 @@ int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t 
     d_queries = e.d_q32;
   }
   e.last_q32 = d_queries;
-  int rc = e.enqueue(d_queries, nq, k, d_idx, d_score, s);
+  int rc = (e.prm.flags & AES_FLAG_GRAPHS) ? e.enqueue_graph(d_queries, nq, k, d_idx, d_score, s)
+                                           : e.enqueue(d_queries, nq, k, d_idx, d_score, s);
   if (rc) return rc;
   e.last_nq = nq;
   e.last_k = k;

@@ -43,6 +43,7 @@ EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", 
            "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact"]
 
 FLAG_PROFILE = 1
+FLAG_GRAPHS = 2
 
 
 class AesError(RuntimeError):

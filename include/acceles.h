@@ -68,6 +68,9 @@ typedef struct aes_params {
 
 /* params.flags bits */
 #define AES_FLAG_PROFILE 1u /* time every candidate-pass launch with CUDA events on its stream */
+#define AES_FLAG_GRAPHS 2u  /* replay each batch's launch sequence as a CUDA graph (captured once
+                               per set of buffers, batch size and K); profiling events are
+                               not recorded inside graphs */
 
 typedef struct aes_stats {
   uint64_t launches;       /* kernels launched by the engine since the last reset */
