@@ -100,6 +100,17 @@ struct Engine {
   uint16_t* d_csr_col = nullptr;
   float* d_csr_val = nullptr;
 
+  // ---- configuration: selection geometry and per-batch buffers (aes_retune may change these) --
+  struct Config {
+    aes_params p{};
+    uint32_t split = 1, slice = 0, ntop = 0, nslots = 0, npow2 = 0, ck_eff = 0, cap = 0;
+    uint32_t ss = 1, n_sample_tiles = 0, n_sample_rows = 0, maxB = 1;
+    std::vector<uint32_t> sample_first, part_begin, part_r;
+    size_t plan = 0;  // device bytes of the configuration's buffers
+  };
+  Config cur;
+  bool configured = false;
+
   uint32_t ss = 1, n_sample_tiles = 0, n_sample_rows = 0;
   uint32_t* d_sample_first = nullptr;
   uint32_t* d_part_sample_begin = nullptr;
@@ -156,7 +167,7 @@ struct Engine {
   double prof_ms = 0.0;
   uint64_t prof_n = 0;
 
-  int plain_grid = 0;
+  int plain_grid = 0, smem_optin = 0;
   size_t plain_smem = 0, final_smem = 0;
   // batched pass
   uint32_t* d_qtab = nullptr;     // [blocks][cols][32] words
@@ -164,23 +175,47 @@ struct Engine {
   size_t batch_smem = 0;
   uint32_t batch_mode = 0;        // 0 auto, 1 never, else always
   bool last_batched = false;
-  size_t bytes = 0;
-  std::vector<void*> allocs;
+  std::vector<uint32_t> h_tile_rowbase;  // host copy: sample geometry is derived from it
+  size_t bytes = 0, mat_bytes = 0, cfg_bytes = 0;
+  std::vector<void*> allocs, cfg_allocs;
 
   ~Engine() { release(); }
+
+  void drop_graphs() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
+  }
+
+  void free_config() {
+    drop_graphs();
+    for (void* p : cfg_allocs) cudaFree(p);
+    cfg_allocs.clear();
+    if (h_q32) cudaFreeHost(h_q32);
+    if (h_status) cudaFreeHost(h_status);
+    h_q32 = nullptr;
+    h_status = nullptr;
+    d_sample_first = d_part_sample_begin = d_part_r = nullptr;
+    d_q32 = nullptr;
+    d_q8 = nullptr;
+    d_sample_keys = d_thr = d_cnt = d_cand = d_cand_key = d_status = d_out_idx = nullptr;
+    d_surv = nullptr;
+    d_out_score = nullptr;
+    d_exact_cand = d_exact_key = d_qtab = nullptr;
+    bytes -= cfg_bytes;
+    cfg_bytes = 0;
+    configured = false;
+    nq_loaded = 0;
+    ran = false;
+    last_from_device = false;
+  }
 
   void release() {
     if (device >= 0) cudaSetDevice(device);
     for (cudaEvent_t ev : prof_ev) cudaEventDestroy(ev);
     prof_ev.clear();
-    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
-    graphs.clear();
+    free_config();
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
-    if (h_q32) cudaFreeHost(h_q32);
-    if (h_status) cudaFreeHost(h_status);
-    h_q32 = nullptr;
-    h_status = nullptr;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -189,7 +224,7 @@ struct Engine {
   }
 
   template <class T>
-  int dalloc(T** p, size_t n) {
+  int dalloc(T** p, size_t n, bool cfg = false) {
     size_t b = std::max<size_t>(n * sizeof(T), 16);
     void* q = nullptr;
     cudaError_t e = cudaMalloc(&q, b);
@@ -197,13 +232,17 @@ struct Engine {
       cudaGetLastError();
       return fail(AES_ERR_NOMEM, std::string("cudaMalloc refused: ") + cudaGetErrorString(e));
     }
-    allocs.push_back(q);
+    (cfg ? cfg_allocs : allocs).push_back(q);
+    (cfg ? cfg_bytes : mat_bytes) += b;
     bytes += b;
     *p = reinterpret_cast<T*>(q);
     return AES_OK;
   }
 
   int build(const HostCSR& m, const aes_params& p);
+  int plan_config(const aes_params& p, Config* c) const;
+  int apply_config(const Config& c);
+  int retune(const aes_params& p);
   int enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
               cudaStream_t s);
   int enqueue_graph(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
@@ -227,6 +266,188 @@ int Engine::collect_profile() {
   return AES_OK;
 }
 
+// Device bytes of the matrix itself: Ultra-CSR tiles, tile row bases, per-row scales, the FP32
+// CSR of the exact pass and the slow path's key array.
+static size_t matrix_plan(uint64_t tiles, uint32_t rows, uint64_t nnz, uint32_t quant) {
+  size_t plan = tiles * (size_t)kTileBytes + (tiles + 1) * 4;
+  plan += (quant == AES_QUANT_UNSIGNED_ROW) ? rows * 4ull : 0;
+  plan += (rows + 1) * 4ull + nnz * 6ull;
+  plan += rows * 4ull;
+  return plan;
+}
+
+// Host-only: selection geometry, sample tiles, per-partition sample ranks and the device bytes
+// of the configuration's buffers.  Needs rows, cols, tiles and h_tile_rowbase.
+int Engine::plan_config(const aes_params& p, Config* c) const {
+  c->p = p;
+  const uint32_t S = p.split <= 1 ? 1 : p.split;
+  c->split = S;
+  c->slice = rows / S;
+  c->ntop = p.ck / S;
+  c->nslots = S * c->ntop;
+  c->npow2 = 1;
+  while (c->npow2 < c->nslots) c->npow2 <<= 1;
+  c->ck_eff = 0;
+  std::vector<uint32_t> prow(S);
+  for (uint32_t q = 0; q < S; q++) {
+    uint32_t r0 = q * c->slice, r1 = (q == S - 1) ? rows : (q + 1) * c->slice;
+    prow[q] = r1 - r0;
+    c->ck_eff += std::min(c->ntop, prow[q]);
+  }
+
+  // sample tiles: every ss-th tile, with the rows each one owns
+  if (p.sample_stride) c->ss = p.sample_stride;
+  else c->ss = tiles <= 64 ? 1 : (tiles <= 16384 ? 64 : 256);
+  const uint32_t ss_ = c->ss;
+  c->n_sample_tiles = (uint32_t)((tiles + ss_ - 1) / ss_);
+  auto owned_begin = [&](uint64_t t) -> uint64_t {
+    if (t >= tiles) return rows;
+    return t == 0 ? 0 : (uint64_t)h_tile_rowbase[t] + 1;
+  };
+  c->sample_first.assign(c->n_sample_tiles, 0);
+  std::vector<uint64_t> s_begin(c->n_sample_tiles), s_end(c->n_sample_tiles);
+  uint64_t pre = 0;
+  for (uint32_t s = 0; s < c->n_sample_tiles; s++) {
+    uint64_t t = (uint64_t)s * ss_;
+    uint64_t b = owned_begin(t), e = std::max(b, owned_begin(t + 1));
+    s_begin[s] = b;
+    s_end[s] = e;
+    c->sample_first[s] = (uint32_t)(b - pre);
+    pre += e - b;
+  }
+  c->n_sample_rows = (uint32_t)pre;
+  // sample index range of each partition
+  c->part_begin.assign(S + 1, 0);
+  {
+    uint32_t s = 0;
+    uint64_t idx = 0;  // sample rows before s_begin[s]
+    for (uint32_t q = 0; q <= S; q++) {
+      uint64_t rb = (q == S) ? rows : (uint64_t)q * c->slice;
+      while (s < c->n_sample_tiles && s_end[s] <= rb) { idx += s_end[s] - s_begin[s]; s++; }
+      uint64_t cc = idx;
+      if (s < c->n_sample_tiles && s_begin[s] < rb) cc += rb - s_begin[s];
+      c->part_begin[q] = (uint32_t)cc;
+    }
+    c->part_begin[S] = c->n_sample_rows;
+  }
+  // r = smallest rank whose binomial tail is below 1e-12: the r-th largest sample key is then
+  // below the partition's ntop-th largest key except with that probability
+  c->part_r.assign(S, 0);
+  size_t cap_need = 1024;
+  for (uint32_t q = 0; q < S; q++) {
+    uint32_t ns = c->part_begin[q + 1] - c->part_begin[q];
+    double f = prow[q] ? (double)ns / (double)prow[q] : 1.0;
+    uint32_t n1 = c->ntop ? c->ntop - 1 : 0;
+    uint32_t r = 1;
+    if (f >= 1.0) r = std::max<uint32_t>(c->ntop, 1);
+    else {
+      r = (uint32_t)std::floor(n1 * f);
+      while (r <= n1 && binom_tail(n1, f, r) > 1e-12) r++;
+      r = std::max<uint32_t>(r, 1);
+    }
+    c->part_r[q] = r;
+    double expect = f > 0 ? (double)r / f : (double)prow[q];
+    size_t cc = (size_t)std::min<double>((double)prow[q], 4.0 * expect + 4.0 * c->ntop + 1024.0);
+    cap_need = std::max(cap_need, cc);
+  }
+  c->cap = (uint32_t)std::min<size_t>(cap_need, (size_t)rows);
+  if (c->cap == 0) c->cap = 1;
+
+  c->maxB = std::max<uint32_t>(p.max_batch, 1);
+  const size_t maxB = c->maxB;
+  const size_t nblk = (maxB + kBatchQ - 1) / kBatchQ;
+  size_t plan = (c->n_sample_tiles + 2ull * S + 2) * 4;
+  plan += nblk * kBatchQ * (size_t)c->n_sample_rows * 4;
+  plan += maxB * (ld32 * 4ull + ld8 + S * 8ull + (size_t)S * c->cap * 8 + c->nslots * 8ull + 4 +
+                  p.k_max * 8ull);
+  plan += nblk * cols * 128;
+  plan += p.k_max * 8ull;
+  c->plan = plan;
+
+  const size_t stage = (size_t)((P + 3) / 4) * 32 * 16;
+  const size_t psmem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
+                       (S > 1 && S <= kThrSmemMax ? S * 4ull : 0ull);
+  if (psmem > (size_t)smem_optin)
+    return fail(AES_ERR_UNSUPPORTED, "shared memory of the candidate pass exceeds the device limit");
+  return AES_OK;
+}
+
+// Allocates the configuration's buffers, uploads its sample metadata and sets launch geometry.
+int Engine::apply_config(const Config& c) {
+  split = c.split;
+  slice = c.slice;
+  ntop = c.ntop;
+  nslots = c.nslots;
+  npow2 = c.npow2;
+  ck_eff = c.ck_eff;
+  cap = c.cap;
+  ss = c.ss;
+  n_sample_tiles = c.n_sample_tiles;
+  n_sample_rows = c.n_sample_rows;
+  maxB = c.maxB;
+  const aes_params& p = c.p;
+
+  int rc2 = 0;
+#define AES_AL(ptr, n) if ((rc2 = dalloc(&(ptr), (n), true)) != AES_OK) return rc2
+  AES_AL(d_sample_first, std::max<uint32_t>(n_sample_tiles, 1));
+  AES_AL(d_part_sample_begin, split + 1);
+  AES_AL(d_part_r, split);
+  AES_AL(d_q32, (size_t)maxB * ld32);
+  AES_AL(d_q8, (size_t)maxB * ld8);
+  // batched passes write sample keys per block of kBatchQ queries: pad to whole blocks
+  const size_t maxB_blk = (size_t)((maxB + kBatchQ - 1) / kBatchQ) * kBatchQ;
+  AES_AL(d_sample_keys, maxB_blk * std::max<uint32_t>(n_sample_rows, 1));
+  AES_AL(d_thr, (size_t)maxB * split);
+  AES_AL(d_cnt, (size_t)maxB * split);
+  AES_AL(d_surv, (size_t)maxB * split * cap);
+  AES_AL(d_cand, (size_t)maxB * std::max<uint32_t>(nslots, 1));
+  AES_AL(d_cand_key, (size_t)maxB * std::max<uint32_t>(nslots, 1));
+  AES_AL(d_status, maxB);
+  AES_AL(d_out_idx, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 32);
+  AES_AL(d_exact_cand, std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_exact_key, std::max<uint32_t>(p.k_max, 1));
+#undef AES_AL
+  AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
+  AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
+  if (n_sample_tiles)
+    AES_CK(cudaMemcpy(d_sample_first, c.sample_first.data(), n_sample_tiles * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemcpy(d_part_sample_begin, c.part_begin.data(), (split + 1) * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemcpy(d_part_r, c.part_r.data(), split * 4ull, cudaMemcpyHostToDevice));
+  AES_CK(cudaMemset(d_q32, 0, (size_t)maxB * ld32 * 4));
+
+  // ---- launch geometry ---------------------------------------------------------------------
+  {
+    size_t stage = (size_t)((P + 3) / 4) * 32 * 16;
+    plain_smem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
+                 (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
+  }
+  int occ = 0;
+  AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), kThreadsPlain, plain_smem));
+  plain_grid = std::max(1, occ) * sm_count;
+  batch_mode = p.batch_tile;
+  batch_warps_n = batch_warps((int)bits, cols, split);
+  if (batch_warps_n < 1) batch_mode = 1;  // query table does not fit: plain passes only
+  if (batch_mode != 1) {
+    batch_smem = batch_smem_bytes((int)bits, cols, split, batch_warps_n);
+    int occb = 0;
+    AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occb, (const void*)pick_batch((int)bits, sgn, MODE_FILTER), batch_warps_n * 32, batch_smem));
+    batch_grid = std::max(1, occb) * sm_count;
+  }
+  {
+    uint32_t kp = 1;
+    while (kp < p.k_max) kp <<= 1;
+    final_smem = ((cols * 4 + 15) & ~15u) + (size_t)std::max(npow2, kp) * 8;
+  }
+  prm = p;
+  cur = c;
+  configured = true;
+  return AES_OK;
+}
+
 int Engine::build(const HostCSR& m, const aes_params& p) {
   prm = p;
   device = p.device;
@@ -238,6 +459,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   if (device < 0 || device >= ndev) return fail(AES_ERR_INVALID, "device ordinal out of range");
   AES_CK(cudaSetDevice(device));
   AES_CK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+  AES_CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
   AES_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   AES_CK(cudaEventCreate(&ev0));
   AES_CK(cudaEventCreate(&ev1));
@@ -249,6 +471,8 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   sgn = (quant == AES_QUANT_SYM_GLOBAL);
   nnz = m.ptr[rows];
   if (nnz >= 0xFFFFFFFFull) return fail(AES_ERR_UNSUPPORTED, "nnz must be below 2^32");
+  ld32 = (cols + 3) & ~3u;
+  ld8 = (cols + 15) & ~15u;
 
   PackedMatrix pm;
   int rc = quantize_and_pack(m, p, &pm);
@@ -258,92 +482,14 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   packets = pm.packets;
   tiles = pm.tiles;
   if (tiles >= 0xFFFFFFFFull) return fail(AES_ERR_UNSUPPORTED, "matrix too large");
+  h_tile_rowbase = pm.tile_rowbase;
 
-  // ---- selection geometry ----------------------------------------------------------------
-  split = p.split <= 1 ? 1 : p.split;
-  slice = rows / split;
-  ntop = p.ck / split;
-  nslots = split * ntop;
-  npow2 = 1;
-  while (npow2 < nslots) npow2 <<= 1;
-  ck_eff = 0;
-  std::vector<uint32_t> prow(split);
-  for (uint32_t q = 0; q < split; q++) {
-    uint32_t r0 = q * slice, r1 = (q == split - 1) ? rows : (q + 1) * slice;
-    prow[q] = r1 - r0;
-    ck_eff += std::min(ntop, prow[q]);
-  }
+  Config c;
+  rc = plan_config(p, &c);
+  if (rc) return rc;
 
-  // ---- sample tiles -------------------------------------------------------------------------
-  if (p.sample_stride) ss = p.sample_stride;
-  else ss = tiles <= 64 ? 1 : (tiles <= 16384 ? 64 : 256);
-  n_sample_tiles = (uint32_t)((tiles + ss - 1) / ss);
-  auto owned_begin = [&](uint64_t t) -> uint64_t {
-    if (t >= tiles) return rows;
-    return t == 0 ? 0 : (uint64_t)pm.tile_rowbase[t] + 1;
-  };
-  std::vector<uint32_t> sample_first(n_sample_tiles);
-  std::vector<uint64_t> s_begin(n_sample_tiles), s_end(n_sample_tiles);
-  uint64_t pre = 0;
-  for (uint32_t s = 0; s < n_sample_tiles; s++) {
-    uint64_t t = (uint64_t)s * ss;
-    uint64_t b = owned_begin(t), e = std::max(b, owned_begin(t + 1));
-    s_begin[s] = b;
-    s_end[s] = e;
-    sample_first[s] = (uint32_t)(b - pre);
-    pre += e - b;
-  }
-  n_sample_rows = (uint32_t)pre;
-  // sample index range of each partition
-  std::vector<uint32_t> part_begin(split + 1, 0);
-  {
-    uint32_t s = 0;
-    uint64_t idx = 0;  // sample rows before s_begin[s]
-    for (uint32_t q = 0; q <= split; q++) {
-      uint64_t rb = (q == split) ? rows : (uint64_t)q * slice;
-      // count sample rows with row < rb
-      while (s < n_sample_tiles && s_end[s] <= rb) { idx += s_end[s] - s_begin[s]; s++; }
-      uint64_t c = idx;
-      if (s < n_sample_tiles && s_begin[s] < rb) c += rb - s_begin[s];
-      part_begin[q] = (uint32_t)c;
-    }
-    part_begin[split] = n_sample_rows;
-  }
-  std::vector<uint32_t> part_r(split);
-  size_t cap_need = 1024;
-  for (uint32_t q = 0; q < split; q++) {
-    uint32_t ns = part_begin[q + 1] - part_begin[q];
-    double f = prow[q] ? (double)ns / (double)prow[q] : 1.0;
-    uint32_t n1 = ntop ? ntop - 1 : 0;
-    uint32_t r = 1;
-    if (f >= 1.0) r = std::max<uint32_t>(ntop, 1);
-    else {
-      r = (uint32_t)std::floor(n1 * f);
-      while (r <= n1 && binom_tail(n1, f, r) > 1e-12) r++;
-      r = std::max<uint32_t>(r, 1);
-    }
-    part_r[q] = r;
-    double expect = f > 0 ? (double)r / f : (double)prow[q];
-    size_t c = (size_t)std::min<double>((double)prow[q], 4.0 * expect + 4.0 * ntop + 1024.0);
-    cap_need = std::max(cap_need, c);
-  }
-  cap = (uint32_t)std::min<size_t>(cap_need, (size_t)rows);
-  if (cap == 0) cap = 1;
-
-  // ---- memory plan and admission ------------------------------------------------------------
-  maxB = std::max<uint32_t>(p.max_batch, 1);
-  ld32 = (cols + 3) & ~3u;
-  ld8 = (cols + 15) & ~15u;
-  size_t plan = 0;
-  plan += tiles * (size_t)kTileBytes + (tiles + 1) * 4;
-  plan += (quant == AES_QUANT_UNSIGNED_ROW) ? rows * 4ull : 0;
-  plan += (rows + 1) * 4ull + nnz * 6ull;
-  plan += (n_sample_tiles + 2ull * split + 2) * 4;
-  plan += (size_t)((maxB + kBatchQ - 1) / kBatchQ) * kBatchQ * (size_t)n_sample_rows * 4;
-  plan += (size_t)maxB * (ld32 * 4ull + ld8 + split * 8ull +
-                          (size_t)split * cap * 8 + nslots * 8ull + 4 + p.k_max * 8ull);
-  plan += rows * 4ull;  // slow-path key array
-  plan += (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 128;
+  // ---- memory plan and admission: nothing is allocated unless all of it fits ---------------
+  const size_t plan = matrix_plan(tiles, rows, nnz, quant) + c.plan;
   if (p.mem_limit && plan > p.mem_limit)
     return fail(AES_ERR_NOMEM, "matrix needs " + std::to_string(plan) +
                                    " device bytes, over the handle limit " +
@@ -362,29 +508,8 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_AL(d_csr_ptr, rows + 1);
   AES_AL(d_csr_col, std::max<uint64_t>(nnz, 1));
   AES_AL(d_csr_val, std::max<uint64_t>(nnz, 1));
-  AES_AL(d_sample_first, std::max<uint32_t>(n_sample_tiles, 1));
-  AES_AL(d_part_sample_begin, split + 1);
-  AES_AL(d_part_r, split);
-  AES_AL(d_q32, (size_t)maxB * ld32);
-  AES_AL(d_q8, (size_t)maxB * ld8);
-  // batched passes write sample keys per block of kBatchQ queries: pad to whole blocks
-  const size_t maxB_blk = (size_t)((maxB + kBatchQ - 1) / kBatchQ) * kBatchQ;
-  AES_AL(d_sample_keys, maxB_blk * std::max<uint32_t>(n_sample_rows, 1));
-  AES_AL(d_thr, (size_t)maxB * split);
-  AES_AL(d_cnt, (size_t)maxB * split);
-  AES_AL(d_surv, (size_t)maxB * split * cap);
-  AES_AL(d_cand, (size_t)maxB * std::max<uint32_t>(nslots, 1));
-  AES_AL(d_cand_key, (size_t)maxB * std::max<uint32_t>(nslots, 1));
-  AES_AL(d_status, maxB);
-  AES_AL(d_out_idx, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
-  AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_allkeys, rows);
-  AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 32);
-  AES_AL(d_exact_cand, std::max<uint32_t>(p.k_max, 1));
-  AES_AL(d_exact_key, std::max<uint32_t>(p.k_max, 1));
 #undef AES_AL
-  AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
-  AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
 
   // ---- upload -----------------------------------------------------------------------------------
   std::vector<uint32_t> ptr32(rows + 1);
@@ -401,54 +526,59 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     AES_CK(cudaMemcpy(d_csr_col, col16.data(), nnz * 2, cudaMemcpyHostToDevice));
     AES_CK(cudaMemcpy(d_csr_val, m.val.data(), nnz * 4, cudaMemcpyHostToDevice));
   }
-  if (n_sample_tiles)
-    AES_CK(cudaMemcpy(d_sample_first, sample_first.data(), n_sample_tiles * 4ull, cudaMemcpyHostToDevice));
-  AES_CK(cudaMemcpy(d_part_sample_begin, part_begin.data(), (split + 1) * 4ull, cudaMemcpyHostToDevice));
-  AES_CK(cudaMemcpy(d_part_r, part_r.data(), split * 4ull, cudaMemcpyHostToDevice));
-  AES_CK(cudaMemset(d_q32, 0, (size_t)maxB * ld32 * 4));
 
-  // ---- launch geometry ---------------------------------------------------------------------
-  {
-    size_t stage = (size_t)((P + 3) / 4) * 32 * 16;
-    plain_smem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
-                 (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
-  }
   // the shared-memory limit is an attribute of the kernel, shared by every handle: raise it to
   // the device maximum once instead of to this handle's size
-  int smem_optin = 0;
-  AES_CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-  if (plain_smem > (size_t)smem_optin) return fail(AES_ERR_UNSUPPORTED, "shared memory of the candidate pass exceeds the device limit");
   for (int mode = 0; mode < 3; mode++) {
     PlainKernel kf = pick_plain((int)bits, sgn, mode);
     AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 smem_optin));
   }
-  int occ = 0;
-  AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), kThreadsPlain, plain_smem));
-  plain_grid = std::max(1, occ) * sm_count;
-  batch_mode = p.batch_tile;
-  batch_warps_n = batch_warps((int)bits, cols, split);
-  if (batch_warps_n < 1) batch_mode = 1;  // query table does not fit: plain passes only
-  if (batch_mode != 1) {
-    batch_smem = batch_smem_bytes((int)bits, cols, split, batch_warps_n);
-    for (int mode = 0; mode < 2; mode++) {
-      BatchKernel kf = pick_batch((int)bits, sgn, mode);
-      AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem_optin));
-    }
-    int occb = 0;
-    AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &occb, (const void*)pick_batch((int)bits, sgn, MODE_FILTER), batch_warps_n * 32, batch_smem));
-    batch_grid = std::max(1, occb) * sm_count;
-  }
-  {
-    uint32_t kp = 1;
-    while (kp < p.k_max) kp <<= 1;
-    final_smem = ((cols * 4 + 15) & ~15u) + (size_t)std::max(npow2, kp) * 8;
+  for (int mode = 0; mode < 2; mode++) {
+    BatchKernel kf = pick_batch((int)bits, sgn, mode);
+    AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smem_optin));
   }
   AES_CK(cudaFuncSetAttribute((const void*)k_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               smem_optin));
+  rc = apply_config(c);
+  if (rc) return rc;
+  AES_CK(cudaDeviceSynchronize());
+  return AES_OK;
+}
+
+// Re-plans CK, split, sample stride, batch tile, k_max, max_batch, flags and the query quantiser
+// of a resident matrix without packing it again.  The old buffers are freed first; if the new
+// ones cannot be had, the old configuration is restored and the error returned.
+int Engine::retune(const aes_params& p) {
+  if (p.bits != prm.bits || p.quant != prm.quant || p.pack_parts != prm.pack_parts ||
+      p.seed != prm.seed || p.device != prm.device)
+    return fail(AES_ERR_INVALID,
+                "bits, quant, pack_parts, seed and device are fixed by the packed matrix");
+  AES_CK(cudaSetDevice(device));
+  Config c;
+  int rc = plan_config(p, &c);
+  if (rc) return rc;
+  if (p.mem_limit && mat_bytes + c.plan > p.mem_limit)
+    return fail(AES_ERR_NOMEM, "configuration needs " + std::to_string(mat_bytes + c.plan) +
+                                   " device bytes, over the handle limit " +
+                                   std::to_string(p.mem_limit));
+  AES_CK(cudaDeviceSynchronize());  // runs on caller streams may still read the old buffers
+  size_t freeb = 0, totalb = 0;
+  AES_CK(cudaMemGetInfo(&freeb, &totalb));
+  if (c.plan + (64ull << 20) > freeb + cfg_bytes)
+    return fail(AES_ERR_NOMEM, "configuration needs " + std::to_string(c.plan) +
+                                   " device bytes, " + std::to_string(freeb + cfg_bytes) +
+                                   " available");
+  Config old = cur;
+  free_config();
+  rc = apply_config(c);
+  if (rc) {
+    std::string why = last_error_cstr();
+    free_config();
+    if (apply_config(old) != AES_OK) free_config();
+    return fail(rc, why);
+  }
   AES_CK(cudaDeviceSynchronize());
   return AES_OK;
 }
@@ -731,6 +861,9 @@ int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cud
 // =============================================================================================
 using aes::Engine;
 
+static const char* const kUnconfigured =
+    "the handle has no configuration: a failed aes_retune could not restore the previous one";
+
 struct aes_handle {
   Engine e;
 };
@@ -851,6 +984,13 @@ int aes_destroy(aes_handle* h) {
   return AES_OK;
 }
 
+int aes_retune(aes_handle* h, const aes_params* p) {
+  if (!h) return aes::fail(AES_ERR_INVALID, "NULL handle");
+  int rc = validate_params(p, h->e.rows, h->e.cols);
+  if (rc) return rc;
+  return h->e.retune(*p);
+}
+
 int aes_get_info(const aes_handle* h, aes_info* info) {
   if (!h || !info) return aes::fail(AES_ERR_INVALID, "NULL argument");
   const Engine& e = h->e;
@@ -878,6 +1018,7 @@ int aes_get_info(const aes_handle* h, aes_info* info) {
 int aes_set_query(aes_handle* h, const float* q, uint32_t nq) {
   if (!h || !q) return aes::fail(AES_ERR_INVALID, "NULL argument");
   Engine& e = h->e;
+  if (!e.configured) return aes::fail(AES_ERR_STATE, kUnconfigured);
   if (nq == 0 || nq > e.maxB) return aes::fail(AES_ERR_INVALID, "nq must be in [1, max_batch]");
   cudaSetDevice(e.device);
   for (uint32_t i = 0; i < nq; i++) std::memcpy(e.h_q32 + (size_t)i * e.ld32, q + (size_t)i * e.cols, e.cols * 4ull);
@@ -921,6 +1062,7 @@ int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t 
                    uint32_t* d_idx, float* d_score, void* stream) {
   if (!h || !d_queries || !d_idx || !d_score) return aes::fail(AES_ERR_INVALID, "NULL argument");
   Engine& e = h->e;
+  if (!e.configured) return aes::fail(AES_ERR_STATE, kUnconfigured);
   if (nq == 0 || nq > e.maxB) return aes::fail(AES_ERR_INVALID, "nq must be in [1, max_batch]");
   if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
   cudaSetDevice(e.device);
@@ -1033,6 +1175,7 @@ int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score
 int aes_score_all(aes_handle* h, const float* q, uint32_t* keys) {
   if (!h || !q || !keys) return aes::fail(AES_ERR_INVALID, "NULL argument");
   Engine& e = h->e;
+  if (!e.configured) return aes::fail(AES_ERR_STATE, kUnconfigured);
   cudaSetDevice(e.device);
   std::memcpy(e.h_q32, q, e.cols * 4ull);
   AES_CK(cudaMemcpyAsync(e.d_q32, e.h_q32, e.ld32 * 4ull, cudaMemcpyHostToDevice, e.stream));
@@ -1146,6 +1289,7 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
   using namespace aes::dev;
   if (!h || !d_query || !d_idx || !d_score) return aes::fail(AES_ERR_INVALID, "NULL argument");
   aes::Engine& e = h->e;
+  if (!e.configured) return aes::fail(AES_ERR_STATE, kUnconfigured);
   if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
   AES_CK(cudaSetDevice(e.device));
   const NoAllocLayout L = noalloc_layout(e);

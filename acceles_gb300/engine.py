@@ -40,7 +40,8 @@ GEN_FIXED_UNIFORM = 3
 
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
            "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
-           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact"]
+           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact",
+           "aes_retune"]
 
 FLAG_PROFILE = 1
 FLAG_GRAPHS = 2
@@ -143,6 +144,8 @@ def load(build_if_missing: bool = True):
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.aes_run_exact.restype = ctypes.c_int
     L.aes_run_exact.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _u32p, _f32p, _u64p]
+    L.aes_retune.restype = ctypes.c_int
+    L.aes_retune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Params)]
     L.aes_get_stats.restype = ctypes.c_int
     L.aes_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats), ctypes.c_int]
     L.aes_score_all.restype = ctypes.c_int
@@ -295,6 +298,20 @@ class SpMV:
         _check(load().aes_run_noalloc(self._h, ctypes.c_void_p(d_query), k,
                                       ctypes.c_void_p(d_idx), ctypes.c_void_p(d_score),
                                       ctypes.c_void_p(stream) if stream else None))
+
+    def retune(self, **changes):
+        """Change ck, split, sample_stride, batch_tile, k_max, max_batch, flags, query_quant or
+        mem_limit without packing the matrix again; loaded queries are dropped."""
+        prm = Params()
+        ctypes.memmove(ctypes.byref(prm), ctypes.byref(self.params), ctypes.sizeof(Params))
+        for k, v in changes.items():
+            if not hasattr(prm, k):
+                raise KeyError(k)
+            setattr(prm, k, v)
+        _check(load().aes_retune(self._h, ctypes.byref(prm)))
+        self.params = prm
+        self._nq = 0
+        self._idx = self._score = None
 
     def finish(self) -> int:
         n = ctypes.c_uint32(0)

@@ -107,6 +107,15 @@ int aes_create_csr(const uint64_t* ptr, const uint32_t* col, const float* val, u
 int aes_destroy(aes_handle* h);
 int aes_get_info(const aes_handle* h, aes_info* info);
 
+/* Change ck, split, sample_stride, batch_tile, k_max, max_batch, flags, query_quant or
+ * mem_limit of a resident matrix without packing it again (bits, quant, pack_parts, seed and
+ * device must equal the creation's: AES_ERR_INVALID otherwise).  Waits for the device, frees
+ * the per-batch buffers and allocates the new ones; loaded queries and results are dropped.
+ * If the new buffers do not fit, the previous configuration is restored and the error returned.
+ * No reference counterpart: the reference fixes these as compile-time constants of the
+ * bitstream (APPROXIMATE_K, SPMV_PARTITIONS: types.hpp:39,149). */
+int aes_retune(aes_handle* h, const aes_params* p);
+
 /* Load nq FP32 queries (row-major [nq][cols], host memory) for the next aes_run.
  * Replaces Q_reset(q_type* vec, int debug) (host_spmv_ucsr.cpp:790-828) / reset(vec)
  * (host_spmv_topk_csr_gpu_int8.cu:288); quantisation happens on the device. */

@@ -1,0 +1,102 @@
+"""aes_retune: a resident matrix re-planned for another CK / split / sample stride / batch tile
+gives the same results as a handle created with those parameters, and the oracle's."""
+import numpy as np
+import pytest
+
+import oracle as orc
+from acceles_gb300 import engine as E
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(rows=30000, cols=1024, bits=4, quant=1, seed=5):
+    ptr, col, val = E.gen_matrix(E.GEN_GAMMA_DEG, rows, cols, 32, 512, seed=seed)
+    return ptr, col, val, orc.Matrix(rows, cols, ptr, col, val, bits, quant)
+
+
+def _queries(cols, nq, seed):
+    rng = np.random.default_rng(seed)
+    Q = rng.random((nq, cols)).astype(np.float32)
+    dens = rng.uniform(0.05, 0.30, nq)
+    Q[rng.random((nq, cols)) >= dens[:, None]] = 0.0
+    return Q
+
+
+@pytest.mark.parametrize("ck,split,stride,tile,nq", [(256, 1, 4, 1, 3), (512, 32, 16, 128, 20),
+                                                      (1024, 8, 0, 0, 20), (128, 1, 1, 128, 17)])
+def test_retune_matches_fresh_handle_and_oracle(ck, split, stride, tile, nq):
+    rows, cols, k = 30000, 1024, 100
+    ptr, col, val, m = _setup(rows, cols)
+    Q = _queries(cols, nq, 3)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=1, ck=1024,
+                 k_max=k, max_batch=4)
+    eng.Q_reset(Q[:4])
+    eng(k=k)
+    eng.retune(ck=ck, split=split, sample_stride=stride, batch_tile=tile, max_batch=nq)
+    inf = eng.info()
+    assert inf["split"] == split and inf["max_batch"] == nq
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    fresh = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=split, ck=ck,
+                   k_max=k, max_batch=nq, sample_stride=stride, batch_tile=tile)
+    fresh.Q_reset(Q)
+    fresh(k=k)
+    fi, fs = fresh.read_topk()
+    assert np.array_equal(idx, fi) and np.array_equal(sc, fs)
+    for i in range(nq):
+        oi, os_, _ = m.two_stage(Q[i], split, ck, k)
+        assert np.array_equal(idx[i, :len(oi)], oi)
+        assert np.array_equal(sc[i, :len(oi)], os_)
+
+
+def test_retune_rejects_packing_changes_and_keeps_working():
+    rows, cols, k = 20000, 1024, 50
+    ptr, col, val, m = _setup(rows, cols, bits=4, quant=1)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=1, ck=512,
+                 k_max=k)
+    Q = _queries(cols, 1, 8)
+    for bad in ({"bits": 8}, {"quant": 0}, {"pack_parts": 4}):
+        with pytest.raises(E.AesError) as ei:
+            eng.retune(**bad)
+        assert ei.value.code == E.AES_ERR_INVALID
+    # over the memory limit: refused before freeing, the old configuration still serves
+    with pytest.raises(E.AesError) as ei:
+        eng.retune(mem_limit=1 << 20)
+    assert ei.value.code == E.AES_ERR_NOMEM
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    oi, os_, _ = m.two_stage(Q[0], 1, 512, k)
+    assert np.array_equal(idx[0, :len(oi)], oi) and np.array_equal(sc[0, :len(oi)], os_)
+    # a retune drops loaded queries
+    eng.retune(ck=256)
+    with pytest.raises(E.AesError) as ei:
+        eng(k=k)
+    assert ei.value.code == E.AES_ERR_STATE
+
+
+def test_autotune_reaches_target_and_leaves_handle_tuned():
+    from acceles_gb300 import autotune as AT
+    rows, cols, k = 40000, 1024, 100
+    ptr, col, val, m = _setup(rows, cols)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=1, ck=1024,
+                 k_max=k, max_batch=32)
+    Q = AT.sparse_queries(24, cols, 17)
+    res = AT.tune(eng, Q, k, ck_ladder=(128, 256, 512, 1024, 2048), splits=(1, 32),
+                  strides=(0, 16), tiles=(1, 128), reps=1)
+    prm = res["params"]
+    assert eng.info()["split"] == prm["split"]
+    # the chosen configuration reproduces the FP32-only Top-K on every sample query
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    assert np.array_equal(idx, res["exact"])
+    # and matches the oracle's two-stage result for the chosen CK / split
+    for i in range(3):
+        oi, os_, _ = m.two_stage(Q[i], prm["split"], prm["ck"], k)
+        assert np.array_equal(idx[i, :len(oi)], oi) and np.array_equal(sc[i, :len(oi)], os_)
+    # the CK trial before the chosen one (same split) missed the target
+    trials = [t for t in res["ck_trials"] if t["split"] == prm["split"]]
+    assert trials[-1]["ck"] == prm["ck"] and trials[-1]["frac_identical"] == 1.0
+    assert all(t["frac_identical"] < 1.0 for t in trials[:-1])
