@@ -18,6 +18,11 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libacceles.so")
+# the library-SpMV comparison arm lives in its own library so that the engine does not load
+# cuSPARSE: its CUDA unit plus the host helpers it shares with the engine
+BASELINE_LIB = os.path.join(OUT_DIR, "libaes_baseline.so")
+BASELINE_ONLY = ("aes_gpu_baseline.cu",)
+BASELINE_SHARED = ("aes_host.cpp",)
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -59,6 +64,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     hdr_digest = _digest(sorted(headers), "hdr")
     nvcc = _nvcc()
     objs = []
+    obj_of = {}
     jobs = []
     for f in cu + cpp:
         src = os.path.join(CSRC, f)
@@ -67,6 +73,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         key = _digest([src], hdr_digest + " ".join(flags) + sys.platform + os.uname().machine)
         obj = os.path.join(OUT_DIR, f"{f}.{key}.o")
         objs.append(obj)
+        obj_of[f] = obj
         if os.path.exists(obj) and not force:
             continue
         if is_cu:
@@ -85,21 +92,28 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
-    link_key = _digest(objs, "link")
-    stamp = LIB + ".stamp"
-    if os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == link_key and not force:
-        return LIB
-    tmp = LIB + ".tmp"
-    run([nvcc, GENCODE, "-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
-    os.replace(tmp, LIB)
-    with open(stamp, "w") as f:
-        f.write(link_key)
+    eng_objs = [obj_of[f] for f in cu + cpp if f not in BASELINE_ONLY]
+    base_objs = [obj_of[f] for f in BASELINE_ONLY + BASELINE_SHARED if f in obj_of]
+    _link(nvcc, LIB, eng_objs, ["-lcudart", "-lpthread"], force, run)
+    _link(nvcc, BASELINE_LIB, base_objs, ["-lcusparse", "-lcudart", "-lpthread"], force, run)
     # drop objects of older source versions
     keep = set(os.path.basename(o) for o in objs)
     for f in os.listdir(OUT_DIR):
         if f.endswith(".o") and f not in keep:
             os.remove(os.path.join(OUT_DIR, f))
     return LIB
+
+
+def _link(nvcc, lib, objs, libs, force, run):
+    link_key = _digest(objs, "link " + " ".join(libs))
+    stamp = lib + ".stamp"
+    if os.path.exists(lib) and os.path.exists(stamp) and open(stamp).read() == link_key and not force:
+        return
+    tmp = lib + ".tmp"
+    run([nvcc, GENCODE, "-shared", "-o", tmp] + objs + libs)
+    os.replace(tmp, lib)
+    with open(stamp, "w") as f:
+        f.write(link_key)
 
 
 if __name__ == "__main__":

@@ -41,7 +41,7 @@ GEN_FIXED_UNIFORM = 3
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
            "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
            "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact",
-           "aes_retune"]
+           "aes_retune", "aes_read_mtx", "aes_free", "aes_write_mtx", "aes_resparse"]
 
 FLAG_PROFILE = 1
 FLAG_GRAPHS = 2
@@ -144,6 +144,17 @@ def load(build_if_missing: bool = True):
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.aes_run_exact.restype = ctypes.c_int
     L.aes_run_exact.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _u32p, _f32p, _u64p]
+    L.aes_read_mtx.restype = ctypes.c_int
+    L.aes_read_mtx.argtypes = [ctypes.c_char_p, ctypes.c_uint32, _u32p, _u32p, _u64p,
+                               ctypes.POINTER(_u32p), ctypes.POINTER(_u32p), ctypes.POINTER(_f32p)]
+    L.aes_free.restype = None
+    L.aes_free.argtypes = [ctypes.c_void_p]
+    L.aes_write_mtx.restype = ctypes.c_int
+    L.aes_write_mtx.argtypes = [ctypes.c_char_p, _u32p, _u32p, _f32p, ctypes.c_uint32,
+                                ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32]
+    L.aes_resparse.restype = ctypes.c_int
+    L.aes_resparse.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                               ctypes.c_double, _u64p, _u32p, _f32p, ctypes.c_uint64, _u64p]
     L.aes_retune.restype = ctypes.c_int
     L.aes_retune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Params)]
     L.aes_get_stats.restype = ctypes.c_int
@@ -203,6 +214,55 @@ def pack_host(ptr, col, val, rows, cols, **params):
                            ctypes.byref(prm), pk.ctypes.data_as(ctypes.c_void_p), n.value,
                            ctypes.byref(n), _p(trb, _u32p)))
     return pk[: n.value], trb
+
+
+MTX_ZERO_INDEXED = 1
+MTX_SORT = 2
+MTX_KEEP_DIRECTED = 4
+
+
+def read_mtx(path, flags: int = 0):
+    """Matrix Market coordinate file -> (rows, cols, row u32, col u32, val f32) COO."""
+    L = load()
+    rows, cols, nnz = ctypes.c_uint32(0), ctypes.c_uint32(0), ctypes.c_uint64(0)
+    r, c, v = _u32p(), _u32p(), _f32p()
+    _check(L.aes_read_mtx(os.fsencode(path), flags, ctypes.byref(rows), ctypes.byref(cols),
+                          ctypes.byref(nnz), ctypes.byref(r), ctypes.byref(c), ctypes.byref(v)))
+    try:
+        n = nnz.value
+        R = np.ctypeslib.as_array(r, shape=(max(n, 1),))[:n].copy()
+        C = np.ctypeslib.as_array(c, shape=(max(n, 1),))[:n].copy()
+        V = np.ctypeslib.as_array(v, shape=(max(n, 1),))[:n].copy()
+    finally:
+        for p in (r, c, v):
+            L.aes_free(ctypes.cast(p, ctypes.c_void_p))
+    return rows.value, cols.value, R, C, V
+
+
+def write_mtx(path, rows, cols, row, col, val, flags: int = 0):
+    row = np.ascontiguousarray(row, np.uint32)
+    col = np.ascontiguousarray(col, np.uint32)
+    val = np.ascontiguousarray(val, np.float32)
+    _check(load().aes_write_mtx(os.fsencode(path), _p(row, _u32p), _p(col, _u32p),
+                                _p(val, _f32p), rows, cols, row.shape[0], flags))
+
+
+def resparse(ptr, col, val, rows, cols, keep):
+    """ReSparse per-row pruning of a sorted CSR: (ptr u64, col u32, val f32) of the kept entries."""
+    L = load()
+    ptr = np.ascontiguousarray(ptr, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    val = np.ascontiguousarray(val, np.float32)
+    n = ctypes.c_uint64(0)
+    optr = np.zeros(rows + 1, np.uint64)
+    _check(L.aes_resparse(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                          float(keep), _p(optr, _u64p), None, None, 0, ctypes.byref(n)))
+    ocol = np.zeros(max(n.value, 1), np.uint32)
+    oval = np.zeros(max(n.value, 1), np.float32)
+    _check(L.aes_resparse(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                          float(keep), _p(optr, _u64p), _p(ocol, _u32p), _p(oval, _f32p),
+                          n.value, ctypes.byref(n)))
+    return optr, ocol[:n.value], oval[:n.value]
 
 
 class SpMV:

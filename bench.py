@@ -157,6 +157,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-queries", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-gpu-baseline", action="store_true")
     ap.add_argument("--check", type=int, default=2, help="queries checked against the oracle")
     ap.add_argument("--rows", type=int, default=ROWS, help="smaller matrix, for profiling only")
     args = ap.parse_args()
@@ -269,6 +270,18 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_qps = world * Kk * B / e2e_s
 
+    # library-SpMV comparison arm on the same matrix and queries (cuSPARSE SpMV + full sort,
+    # the reference's GPU baseline method), device time per query
+    gpu_lib = None
+    if rank == 0 and not args.no_gpu_baseline:
+        try:
+            from acceles_gb300 import gpu_baseline as G
+            _, _, ms_lib = G.cusparse_topk(ptr, col, val, rows, COLS, Qh[:17], K, device=local)
+            gpu_lib = {"method": "cuSPARSE SpMV (FP32 CSR) + full descending radix sort + first K",
+                       "ms_per_query": ms_lib, "queries_per_s": 1e3 / ms_lib, "queries_timed": 16}
+        except Exception as ex:  # report, do not fail the bench
+            gpu_lib = {"unavailable": str(ex)[:200]}
+
     # correctness of the measured configuration (outside the timed regions)
     line_extra = {}
     if rank == 0:
@@ -320,6 +333,7 @@ def main():
                     "d2h_bytes_per_step": B * K * 8},
             "gpu_launches": st["launches"], "repaired_queries": repaired + st["repaired"] + rep_p + st_p["repaired"],
             "clocks": clk, "clocks_plain": clk_p,
+            "gpu_library_baseline": gpu_lib,
         }
         line.update(line_extra)
         print(json.dumps(line), flush=True)

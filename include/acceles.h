@@ -201,6 +201,37 @@ int aes_pack_host(const uint64_t* ptr, const uint32_t* col, const float* val, ui
 uint64_t aes_gen_matrix(uint32_t kind, uint32_t rows, uint32_t cols, double p0, double p1,
                         uint64_t seed, uint64_t* ptr, uint32_t* col, float* val);
 
+/* ---- Matrix Market files ------------------------------------------------------------------ */
+#define AES_MTX_ZERO_INDEXED 1u  /* indices in the file start at 0 (the reference host reads its
+                                    .mtx files this way: host_spmv_ucsr.cpp:938,969) */
+#define AES_MTX_SORT 2u          /* order entries by (row, col); equal keys keep file order */
+#define AES_MTX_KEEP_DIRECTED 4u /* do not mirror the off-diagonal entries of a symmetric file */
+/* Read a coordinate Matrix Market file (real, integer or pattern; general or symmetric) into a
+ * COO whose arrays the library allocates (release each with aes_free).  Entries come in file
+ * order, then the mirrored off-diagonal entries of a symmetric file; pattern entries read as
+ * 1.0; values are parsed as double and rounded to FP32.  Replaces readMtx + readTuples +
+ * undirect + customSort (utils.hpp:331-492, mmio.hpp), which exit() on errors where this
+ * returns AES_ERR_INVALID (bad banner, entry count, index out of range). */
+int aes_read_mtx(const char* path, uint32_t flags, uint32_t* rows, uint32_t* cols, uint64_t* nnz,
+                 uint32_t** row, uint32_t** col, float** val);
+void aes_free(void* p);
+/* Write a COO as "%%MatrixMarket matrix coordinate real general", a "%" line, the size line
+ * and one "row col value" line per entry (one-based unless AES_MTX_ZERO_INDEXED), values with
+ * 9 significant digits (FP32 values read back exactly).  Replaces write_coo_to_mtx
+ * (quantify_util.py:469-477), which takes the shape from the largest indices instead. */
+int aes_write_mtx(const char* path, const uint32_t* row, const uint32_t* col, const float* val,
+                  uint32_t rows, uint32_t cols, uint64_t nnz, uint32_t flags);
+
+/* ---- ReSparse: per-row pruning before quantisation ---------------------------------------- */
+/* For each row of a CSR (sorted, no duplicate (row, col)): if its smallest nonzero |v| exceeds
+ * the mean |v| of the whole rows x cols matrix (zeros included), keep the row; else keep its
+ * ceil(n * keep) largest |v| (equal |v|: the higher column first), in column order.  Explicit
+ * zeros are dropped.  keep in (0, 1].  out_ptr[rows+1]; pass out_col = out_val = NULL to learn
+ * *out_nnz.  Replaces resparse_spm (quantify_util.py:375-403), a dense-matrix loop in numpy. */
+int aes_resparse(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                 uint32_t cols, double keep, uint64_t* out_ptr, uint32_t* out_col,
+                 float* out_val, uint64_t cap, uint64_t* out_nnz);
+
 #ifdef __cplusplus
 }
 #endif

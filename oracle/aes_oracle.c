@@ -574,3 +574,58 @@ double orc_bench_two_stage(const uint64_t* ptr, const uint32_t* col, const float
   free(q); free(jobs); free(th); free(cidx); free(cval); free(cc); free(sel); free(sc);
   return el;
 }
+
+/* ---------------------------------------------------------------------------------------- */
+/* ReSparse (quantify_util.py:375-403)                                                        */
+/* ---------------------------------------------------------------------------------------- */
+
+uint64_t orc_resparse(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                      uint32_t cols, double keep, uint64_t* out_ptr, uint32_t* out_col,
+                      float* out_val) {
+  double sum = 0.0;
+  for (uint64_t e = 0; e < ptr[rows]; e++) sum += fabs((double)val[e]);
+  const double avg = sum / ((double)rows * (double)cols);  /* np.mean(np.abs(spm)) */
+  uint64_t o = 0;
+  out_ptr[0] = 0;
+  for (uint32_t r = 0; r < rows; r++) {
+    uint64_t n = 0;
+    double mn = INFINITY;
+    for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) {
+      if (val[e] == 0.0f) continue;
+      n++;
+      if (fabs((double)val[e]) < mn) mn = fabs((double)val[e]);
+    }
+    if (n > 0 && mn > avg) {
+      for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) {
+        if (val[e] == 0.0f) continue;
+        out_col[o] = col[e];
+        out_val[o] = val[e];
+        o++;
+      }
+    } else if (n > 0) {
+      uint64_t k = (uint64_t)ceil((double)n * keep);
+      if (k > n) k = n;
+      /* mark the k largest |v| one at a time; among equal |v| the higher column wins */
+      unsigned char* take = (unsigned char*)calloc(ptr[r + 1] - ptr[r], 1);
+      for (uint64_t t = 0; t < k; t++) {
+        uint64_t best = UINT64_MAX;
+        for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) {
+          if (val[e] == 0.0f || take[e - ptr[r]]) continue;
+          if (best == UINT64_MAX) { best = e; continue; }
+          const float a = fabsf(val[e]), b = fabsf(val[best]);
+          if (a > b || (a == b && col[e] > col[best])) best = e;
+        }
+        take[best - ptr[r]] = 1;
+      }
+      for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) {
+        if (!take[e - ptr[r]]) continue;
+        out_col[o] = col[e];
+        out_val[o] = val[e];
+        o++;
+      }
+      free(take);
+    }
+    out_ptr[r + 1] = o;
+  }
+  return o;
+}

@@ -137,6 +137,17 @@ double orc_bench_two_stage(const uint64_t* ptr, const uint32_t* col, const float
                            const float* queries, uint32_t nq, int nthreads, double max_seconds,
                            uint32_t* done, uint32_t* out_idx);
 
+/* ReSparse per-row pruning, restating resparse_spm (quantify_util.py:375-403) on a CSR sorted by
+ * (row, col) without duplicates: mean |v| over rows x cols (zeros included, plain double sum in
+ * entry order); a row whose smallest nonzero |v| exceeds the mean is kept whole, else its
+ * ceil(n * keep) largest |v| are kept (equal |v|: higher column first, the order of the
+ * reference's reversed ascending argsort for rows of up to 16 nonzeros), in column order.
+ * Explicit zeros are dropped.  out_ptr[rows+1]; out_col/out_val sized ptr[rows].  Returns the
+ * kept count. */
+uint64_t orc_resparse(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                      uint32_t cols, double keep, uint64_t* out_ptr, uint32_t* out_col,
+                      float* out_val);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,10 @@ Reference anchors (files of zhaijiaqi/AccelES):
   spmv_coo_gold_top_k(_2)             src/fpga/src/gold_algorithms/gold_algorithms.hpp:189-308
   sort_tuples                         src/common/utils/evaluation_utils.hpp:40-62
   Ultra-CSR packet layout             src/fpga/src/ip/fpga_utils.hpp:317-527, types.hpp:151-162
+  resparse_spm                        src/resources/python/quantify/quantify_util.py:375-403
+  ReSparse ratio search               src/resources/python/quantify/datasets/
+                                      search_best_resparse_ratio.py:55-117
+  compt_precision / convergence       src/resources/python/quantify/quantify_util.py:198-219,413-437
 """
 from __future__ import annotations
 
@@ -118,6 +122,9 @@ def lib():
                                           ctypes.c_uint32, ctypes.c_uint32, _f32p,
                                           ctypes.c_uint32, ctypes.c_int, ctypes.c_double, _u32p,
                                           _u32p]
+        L.orc_resparse.restype = ctypes.c_uint64
+        L.orc_resparse.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                   ctypes.c_double, _u64p, _u32p, _f32p]
         _lib = L
     return _lib
 
@@ -145,6 +152,10 @@ def ref_lib():
         R.ref_sort_tuples_i32.argtypes = [ctypes.c_uint32, _u32p, _i32p]
         R.ref_sort_pr_f32.restype = None
         R.ref_sort_pr_f32.argtypes = [ctypes.c_uint32, _f32p, _u32p]
+        R.ref_read_mtx.restype = ctypes.c_uint32
+        R.ref_read_mtx.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, _u32p, _u32p, _u32p, _u32p, _f32p,
+                                   ctypes.c_uint32]
         _ref = R
     return _ref
 
@@ -367,3 +378,83 @@ def np_quantify_vector(v, B, symmetric=True):
     m = max(abs(np.max(v)), abs(np.min(v)))
     v /= m
     return np.clip(np.int32(np.round(M * v)), int(-M) - 1, int(M))
+
+
+# ---------------------------------------------------------------------------------------------
+# ReSparse and its ratio search
+# ---------------------------------------------------------------------------------------------
+
+def resparse(ptr, col, val, rows, cols, keep):
+    """orc_resparse: (ptr u64, col u32, val f32) of the kept entries."""
+    ptr = np.ascontiguousarray(ptr, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    val = np.ascontiguousarray(val, np.float32)
+    n = int(ptr[rows])
+    op = np.zeros(rows + 1, np.uint64)
+    oc = np.zeros(max(n, 1), np.uint32)
+    ov = np.zeros(max(n, 1), np.float32)
+    k = lib().orc_resparse(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                           float(keep), _p(op, _u64p), _p(oc, _u32p), _p(ov, _f32p))
+    return op, oc[:k], ov[:k]
+
+
+TOP_KS = (1, 8, 16, 32, 50, 75, 100)
+TOP_K_WEIGHTS = (1.0, 1 / 8, 1 / 16, 1 / 32, 1 / 50, 1 / 75, 1 / 100)
+
+
+def compt_precision(ref_top_idx, cand):
+    """|set(cand) & set(ref[:K])| / K for K in TOP_KS (quantify_util.py:198-219)."""
+    c = set(int(x) for x in cand)
+    return [len(c & set(int(x) for x in ref_top_idx[:K])) / K for K in TOP_KS]
+
+
+def convergence_metric(precisions):
+    """Weighted sum of the mean precisions (quantify_util.py:413-437)."""
+    n = len(precisions)
+    avg = [sum(p[i] for p in precisions) / n for i in range(len(TOP_KS))]
+    return sum(avg[i] * TOP_K_WEIGHTS[i] for i in range(len(TOP_KS)))
+
+
+def search_keep_ratio(evaluate, accuracy_threshold=0.999, max_epochs=100):
+    """The reference's ReSparse bisection (search_best_resparse_ratio.py:55-117) over an
+    evaluate(keep_ratio, epoch) -> convergence-metric callback.  Returns (converged keep ratio
+    or None, [(epoch, ratio, metric), ...])."""
+    history = []
+    high, low = 1.0, 0.0
+    attempted = set()
+    ratio = 1.0
+    threshold = None
+    for epoch in range(max_epochs):
+        if epoch == 0:
+            ratio = 1.0
+        elif epoch == 1:
+            ratio = (low + high) / 2
+        metric = evaluate(ratio, epoch)
+        attempted.add(ratio)
+        history.append((epoch, ratio, metric))
+        if epoch == 0:
+            threshold = metric * accuracy_threshold
+            continue
+        if metric >= threshold:
+            high = ratio
+        else:
+            low = ratio
+        ratio = round((low + high) / 2, 3)
+        if ratio in attempted:
+            return high, history
+    return None, history
+
+
+def ref_read_mtx(path, directed=0, read_values=True, zero_indexed=False, sort=True, cap=1 << 20):
+    """readMtx of the reference (needs oracle/_ref): (rows, cols, row, col, val)."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("reference library not built")
+    rows, cols = ctypes.c_uint32(0), ctypes.c_uint32(0)
+    r = np.zeros(cap, np.uint32)
+    c = np.zeros(cap, np.uint32)
+    v = np.zeros(cap, np.float32)
+    n = R.ref_read_mtx(os.fsencode(path), directed, int(read_values), int(zero_indexed), int(sort),
+                       ctypes.byref(rows), ctypes.byref(cols), _p(r, _u32p), _p(c, _u32p),
+                       _p(v, _f32p), cap)
+    return rows.value, cols.value, r[:n].copy(), c[:n].copy(), v[:n].copy()

@@ -11,6 +11,8 @@
  *   spmv_coo_gold_top_k     src/fpga/src/gold_algorithms/gold_algorithms.hpp:189-247
  *   spmv_coo_gold4          src/fpga/src/gold_algorithms/gold_algorithms.hpp:141-187
  *   sort_tuples / sort_pr   src/common/utils/evaluation_utils.hpp:16-62
+ *   readMtx                 src/common/utils/utils.hpp:450-492 (with readTuples, undirect,
+ *                           customSort :331-437 and mmio.hpp)
  */
 #include <cmath>
 #include <cstdint>
@@ -23,6 +25,7 @@ using std::log2;
 #include "common/types.hpp"
 #include "common/csc_matrix/csc_matrix.hpp"
 #include "common/utils/evaluation_utils.hpp"
+#include "common/utils/utils.hpp"
 #include "fpga/src/gold_algorithms/gold_algorithms.hpp"
 
 extern "C" {
@@ -64,6 +67,27 @@ void ref_sort_tuples_i32(uint32_t n, uint32_t* idx, int32_t* val) {
 void ref_sort_pr_f32(uint32_t n, const float* val, uint32_t* out_idx) {
   std::vector<index_type> o = sort_pr<float>(n, const_cast<float*>(val));
   for (uint32_t i = 0; i < n; i++) out_idx[i] = o[i];
+}
+
+/* readMtx into caller arrays of capacity cap; returns the entry count (0 when over cap).
+ * The reference exits the process on a malformed file: call it on valid files only. */
+uint32_t ref_read_mtx(const char* path, int directed, int read_values, int zero_indexed,
+                      int sort, uint32_t* rows, uint32_t* cols, uint32_t* row, uint32_t* col,
+                      float* val, uint32_t cap) {
+  std::vector<unsigned> r, c;
+  std::vector<float> v;
+  unsigned nr = 0, nc = 0, nz = 0;
+  readMtx<unsigned, float>(path, &r, &c, &v, &nr, &nc, &nz, directed, read_values != 0, false,
+                           zero_indexed != 0, sort != 0);
+  *rows = nr;
+  *cols = nc;
+  if (r.size() > cap) return 0;
+  for (size_t i = 0; i < r.size(); i++) {
+    row[i] = r[i];
+    col[i] = c[i];
+    val[i] = v[i];
+  }
+  return (uint32_t)r.size();
 }
 
 }  // extern "C"

@@ -18,6 +18,14 @@ Outputs (small .npz files, committed):
   xdecode.npz     the x_decoder known-answer case, flag word 0x20080200
                   (src/fpga/src/x_decoder/test_x_decoder.cpp:6), decoded by increment_array
                   (x_decoder.cpp:5-22) as restated bit by bit below
+  resparse.npz    resparse_spm (quantify_util.py:375-403) run on seeded dense matrices for
+                  several keep ratios; equal |v| never straddle a row's cut (numpy's argsort
+                  orders ties differently per platform, so the reference leaves them unspecified)
+  mtx/*.mtx +     small Matrix Market files written here, and what the reference's readMtx
+  mtx.npz         (src/common/utils/utils.hpp:450-492, compiled in oracle/_ref) returns for them
+                  under the argument combinations the reference uses
+
+  python tests/golden/make_golden.py [--only resparse,mtx]
 """
 from __future__ import annotations
 
@@ -180,17 +188,130 @@ def make_xdecode():
     return {"flags": np.array([flags], np.uint64), "P": np.array([P]), "x": x}
 
 
+RESPARSE_KEEPS = (1.0, 0.9, 0.776, 0.5, 0.05)
+
+
+def _dense_to_csr(m):
+    rows = m.shape[0]
+    ptr = np.zeros(rows + 1, np.uint64)
+    cols, vals = [], []
+    for r in range(rows):
+        nz = np.nonzero(m[r])[0]
+        cols.extend(nz.tolist())
+        vals.extend(m[r, nz].tolist())
+        ptr[r + 1] = ptr[r] + len(nz)
+    return ptr, np.array(cols, np.uint32), np.array(vals, np.float32)
+
+
+def make_resparse(qu, rng):
+    out = {}
+    mats = []
+    # continuous values (no ties): |N(0,1)| at 20% density, and signed N(0,1) at 50%
+    for (r, c, dens, signed) in [(120, 40, 0.2, False), (60, 30, 0.5, True)]:
+        m = rng.standard_normal((r, c)).astype(np.float32)
+        if not signed:
+            m = np.abs(m)
+        m *= (rng.random((r, c)) < dens)
+        mats.append(m)
+    # repeated magnitudes, one value per row repeated only above the cut: rows of 8 nonzeros
+    # whose 3 largest |v| are equal (kept together for every keep >= 0.375) and the rest distinct
+    t = np.zeros((20, 24), np.float32)
+    for r in range(20):
+        cs = rng.choice(24, 8, replace=False)
+        v = np.concatenate([np.full(3, 4.0 + r), rng.uniform(0.01, 1.0, 5)]).astype(np.float32)
+        v *= rng.choice([-1.0, 1.0], 8).astype(np.float32)
+        t[r, cs] = v
+    mats.append(t)
+    for i, m in enumerate(mats):
+        ptr, col, val = _dense_to_csr(m)
+        out[f"m{i}_shape"] = np.array(m.shape, np.uint32)
+        out[f"m{i}_ptr"], out[f"m{i}_col"], out[f"m{i}_val"] = ptr, col, val
+        keeps = RESPARSE_KEEPS if i < 2 else (1.0, 0.776, 0.5, 0.375)
+        out[f"m{i}_keeps"] = np.array(keeps)
+        for j, keep in enumerate(keeps):
+            res = qu.resparse_spm(m.astype(np.float64), keep)
+            p2, c2, v2 = _dense_to_csr(res.astype(np.float32))
+            out[f"m{i}_k{j}_ptr"], out[f"m{i}_k{j}_col"], out[f"m{i}_k{j}_val"] = p2, c2, v2
+    return out
+
+
+MTX_FILES = {
+    "general_1based.mtx": (
+        "%%MatrixMarket matrix coordinate real general\n"
+        "% a comment line\n"
+        "%\n"
+        "7 5 10\n"
+        "3 2 1.5\n1 1 -2e-3\n7 5 3\n2 4 +4.25\n3 1 0.1\n"
+        "1 5 -7.75\n6 3 1e+2\n2 2 0.333333333333\n5 1 -0\n4 4 12\n"),
+    "symmetric_1based.mtx": (
+        "%%MatrixMarket matrix coordinate real symmetric\n"
+        "5 5 7\n"
+        "1 1 2.0\n2 1 -1.0\n3 2 0.5\n3 3 4.0\n5 2 1.25\n4 1 -3.5\n5 5 6\n"),
+    "pattern_1based.mtx": (
+        "%%MatrixMarket matrix coordinate pattern general\n"
+        "4 6 5\n"
+        "1 6\n4 1\n2 3\n3 3\n1 2\n"),
+    "general_0based.mtx": (
+        "%%MatrixMarket matrix coordinate real general\n"
+        "%\n"
+        "6 4 8\n"
+        "0 0 1\n5 3 -2.5\n2 1 0.75\n0 3 8\n4 2 -0.125\n1 1 3\n3 0 9.5\n5 0 1e-3\n"),
+}
+# (file, directed, read_values, zero_indexed, sort) of the reference readMtx; the matching
+# library flags are chosen by the test
+MTX_CASES = [
+    ("general_1based.mtx", 0, 1, 0, 1),
+    ("general_1based.mtx", 0, 1, 0, 0),
+    ("symmetric_1based.mtx", 0, 1, 0, 0),
+    ("symmetric_1based.mtx", 1, 1, 0, 0),
+    ("symmetric_1based.mtx", 0, 1, 0, 1),
+    ("pattern_1based.mtx", 0, 0, 0, 0),
+    ("general_0based.mtx", 0, 1, 1, 0),
+]
+
+
+def make_mtx():
+    import oracle as orc
+    d = os.path.join(HERE, "mtx")
+    os.makedirs(d, exist_ok=True)
+    for name, text in MTX_FILES.items():
+        with open(os.path.join(d, name), "w") as f:
+            f.write(text)
+    out = {}
+    for i, (name, directed, rv, zero, srt) in enumerate(MTX_CASES):
+        rows, cols, r, c, v = orc.ref_read_mtx(os.path.join(d, name), directed, bool(rv),
+                                               bool(zero), bool(srt), cap=64)
+        out[f"c{i}_args"] = np.array([directed, rv, zero, srt], np.int32)
+        out[f"c{i}_name"] = np.array(name)
+        out[f"c{i}_shape"] = np.array([rows, cols], np.uint32)
+        out[f"c{i}_row"], out[f"c{i}_col"], out[f"c{i}_val"] = r, c, v
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-src", default="/root/reference/src")
+    ap.add_argument("--only", default="quantify,split,gold,xdecode,resparse,mtx")
     args = ap.parse_args()
+    only = set(args.only.split(","))
     qu = load_quantify_util(args.ref_src)
     rng = np.random.default_rng(20241203)
-    np.savez_compressed(os.path.join(HERE, "quantify.npz"), **make_quantify(qu, rng))
-    np.savez_compressed(os.path.join(HERE, "split.npz"), **make_split(qu, rng))
-    np.savez_compressed(os.path.join(HERE, "gold.npz"), **make_gold(rng))
-    np.savez_compressed(os.path.join(HERE, "xdecode.npz"), **make_xdecode())
-    for f in ("quantify.npz", "split.npz", "gold.npz", "xdecode.npz"):
+    made = []
+    # the first four share one random stream: generate them together or not at all
+    if only & {"quantify", "split", "gold", "xdecode"}:
+        np.savez_compressed(os.path.join(HERE, "quantify.npz"), **make_quantify(qu, rng))
+        np.savez_compressed(os.path.join(HERE, "split.npz"), **make_split(qu, rng))
+        np.savez_compressed(os.path.join(HERE, "gold.npz"), **make_gold(rng))
+        np.savez_compressed(os.path.join(HERE, "xdecode.npz"), **make_xdecode())
+        made += ["quantify.npz", "split.npz", "gold.npz", "xdecode.npz"]
+    if "resparse" in only:
+        np.savez_compressed(os.path.join(HERE, "resparse.npz"),
+                            **make_resparse(qu, np.random.default_rng(375403)))
+        made.append("resparse.npz")
+    if "mtx" in only:
+        np.savez_compressed(os.path.join(HERE, "mtx.npz"), **make_mtx())
+        made.append("mtx.npz")
+    for f in made:
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -143,3 +143,14 @@ def test_create_without_gpu_fails_cleanly():
     with pytest.raises(E.AesError) as ei:
         E.SpMV(2, 4, row=[0, 1], col=[0, 1], val=[1.0, 1.0])
     assert ei.value.code in (E.AES_ERR_NODEV, E.AES_ERR_CUDA)
+
+
+def test_baseline_library_exports_its_header():
+    from acceles_gb300 import gpu_baseline as G
+    src = open(os.path.join(REPO, "include", "acceles_baseline.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    decl = set(re.findall(r"\b(aes_[a-z_]+)\s*\(", src))
+    assert decl == set(G.EXPORTS)
+    L = G.load()
+    for name in decl:
+        assert hasattr(L, name), name
