@@ -38,23 +38,31 @@ struct BatchArgs {
   uint32_t sample_stride, n_sample_tiles;
 };
 
+// per-warp element records: column byte offsets (u32), values (u8) and row flags (u8) of the 32
+// packets of a tile, plus one zero group of four so the walk can read one group ahead
+template <int B>
+__host__ __device__ constexpr uint32_t batch_rec_elems() {
+  return 32u * packet_elems(B) + 4u;
+}
 template <int B>
 __host__ __device__ constexpr size_t batch_warp_bytes() {
-  // offsets (u32) + values (u8) + flags (u8) for 32 packets
-  return (size_t)32 * packet_elems(B) * 6;
+  return ((size_t)batch_rec_elems<B>() * 6 + 15) & ~(size_t)15;
+}
+__host__ __device__ constexpr size_t batch_warp_bytes_rt(int B) {
+  return (((size_t)32 * packet_elems(B) + 4) * 6 + 15) & ~(size_t)15;
 }
 
 __host__ __device__ inline bool batch_thr_in_smem(uint32_t split) { return split > 1 && split <= 32; }
 
 // warps per CTA that fit next to the query table (and thresholds) in shared memory
 __host__ inline int batch_warps(int B, uint32_t cols, uint32_t split) {
-  const size_t per = (size_t)32 * packet_elems(B) * 6;
+  const size_t per = batch_warp_bytes_rt(B);
   const size_t fixed = (size_t)cols * kBatchQ + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0);
   int w = (int)((kSmemMax - fixed) / per);
   return w > kWarpsBatchMax ? kWarpsBatchMax : w;
 }
 __host__ inline size_t batch_smem_bytes(int B, uint32_t cols, uint32_t split, int warps) {
-  const size_t per = (size_t)32 * packet_elems(B) * 6;
+  const size_t per = batch_warp_bytes_rt(B);
   return (size_t)cols * kBatchQ + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0) +
          (size_t)warps * per;
 }
@@ -82,11 +90,21 @@ struct BatchRows {
   const BatchArgs& a;
   const uint32_t* thr_s;  // [split][128] in smem (split in 2..64), else nullptr
   uint32_t thr4[4];       // split == 1
+  int32_t thr_sc[4];      // split == 1, integer keys: thr4 as signed score bounds
   uint32_t sample_base;
   uint32_t lane;
 
   // the four queries of this lane finished row `row` with integer scores acc[0..3]
   __device__ __forceinline__ void finish(uint32_t row, const int32_t (&acc)[4]) const {
+    if constexpr (MODE == MODE_FILTER) {
+      if (!a.rowscale && a.split <= 1) {
+        // integer keys, one partition: key >= th  <=>  score >= th ^ 0x80000000 (signed)
+        const bool hit = (acc[0] >= thr_sc[0]) | (acc[1] >= thr_sc[1]) | (acc[2] >= thr_sc[2]) |
+                         (acc[3] >= thr_sc[3]);
+        if (__ballot_sync(0xFFFFFFFFu, hit)) append(row, 0, acc, thr4, false);
+        return;
+      }
+    }
     uint32_t key[4];
     if (a.rowscale) {
       const float rs = __ldg(a.rowscale + row);
@@ -116,16 +134,26 @@ struct BatchRows {
         }
       }
       const bool hit = (key[0] >= th[0]) | (key[1] >= th[1]) | (key[2] >= th[2]) | (key[3] >= th[3]);
-      if (__any_sync(0xFFFFFFFFu, hit) && hit) {
+      if (__ballot_sync(0xFFFFFFFFu, hit)) {
+        int32_t k2[4];
 #pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const uint32_t q = 4 * lane + t;
-          if (key[t] >= th[t] && q < a.nq) {
-            const size_t qp = (size_t)(a.q0 + q) * a.split + p;
-            const uint32_t i = atomicAdd(a.cnt + qp, 1u);
-            if (i < a.cap) a.surv[qp * a.cap + i] = make_uint2(key[t], row);
-          }
-        }
+        for (int t = 0; t < 4; t++) k2[t] = (int32_t)key[t];
+        append(row, p, k2, th, true);
+      }
+    }
+  }
+
+  // survivors of a finished row (rare): v[t] is the key (is_key) or the integer score
+  __device__ __forceinline__ void append(uint32_t row, uint32_t p, const int32_t (&v)[4],
+                                      const uint32_t (&th)[4], bool is_key) const {
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const uint32_t key = is_key ? (uint32_t)v[t] : key_i32(v[t]);
+      const uint32_t q = 4 * lane + t;
+      if (key >= th[t] && q < a.nq) {
+        const size_t qp = (size_t)(a.q0 + q) * a.split + p;
+        const uint32_t i = atomicAdd(a.cnt + qp, 1u);
+        if (i < a.cap) a.surv[qp * a.cap + i] = make_uint2(key, row);
       }
     }
   }
@@ -136,13 +164,14 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
                             const BatchRows<MODE>& rows, const uint8_t* qtb,
                             unsigned char* wsm) {
   constexpr int P = packet_elems(B);
-  constexpr int NE = 32 * P;     // elements per tile
-  constexpr int NG = NE / 4;     // groups of four
+  constexpr int NE = 32 * P;                 // elements per tile
+  constexpr int NG = NE / 4;                 // groups of four
+  constexpr uint32_t NR = batch_rec_elems<B>();
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lane4 = lane << 2;
-  uint32_t* offs = reinterpret_cast<uint32_t*>(wsm);            // [NE] col * 128
-  uint8_t* vals = wsm + (size_t)NE * 4;                          // [NE]
-  uint8_t* flg = wsm + (size_t)NE * 5;                           // [NE]
+  uint32_t* offs = reinterpret_cast<uint32_t*>(wsm);            // [NR] col * 128
+  uint8_t* vals = wsm + (size_t)NR * 4;                          // [NR]
+  uint8_t* flg = wsm + (size_t)NR * 5;                           // [NR]
   if (tb >= te) return;
   bool owned = (tb == 0);
   uint32_t row = __ldg(a.tile_rowbase + tb);  // id of the row open before the first entry
@@ -178,23 +207,59 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
     }
     __syncwarp();
     // ---- phase B: lanes = queries ------------------------------------------------------------
+    // The gathers of group g+1 are issued before group g's arithmetic and branches (the zero
+    // group after the last one keeps the read in bounds).  The flag word comes through a
+    // shuffle from lane 0 (every lane holds the same word): branches on it are then known to be
+    // warp-uniform and need no reconvergence bookkeeping.
+    const uint4* O = reinterpret_cast<const uint4*>(offs);
+    const uint32_t* Vg = reinterpret_cast<const uint32_t*>(vals);
+    const uint32_t* Fg = reinterpret_cast<const uint32_t*>(flg);
+    uint32_t Wn[4], v4n, f4n;
+    {
+      const uint4 o4 = O[0];
+      v4n = Vg[0];
+      f4n = __shfl_sync(0xFFFFFFFFu, Fg[0], 0);
+      Wn[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x + lane4));
+      Wn[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y + lane4));
+      Wn[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z + lane4));
+      Wn[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w + lane4));
+    }
 #pragma unroll 2
     for (int g = 0; g < NG; g++) {
-      const uint4 o4 = reinterpret_cast<const uint4*>(offs)[g];
-      const uint32_t v4 = reinterpret_cast<const uint32_t*>(vals)[g];
-      const uint32_t f4 = reinterpret_cast<const uint32_t*>(flg)[g];
-      uint32_t W[4], V[4];
-      W[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x + lane4));
-      W[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y + lane4));
-      W[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z + lane4));
-      W[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w + lane4));
+      const uint32_t W[4] = {Wn[0], Wn[1], Wn[2], Wn[3]};
+      const uint32_t v4 = v4n, f4 = f4n;
+      {
+        const uint4 o4 = O[g + 1];
+        v4n = Vg[g + 1];
+        f4n = __shfl_sync(0xFFFFFFFFu, Fg[g + 1], 0);
+        Wn[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x + lane4));
+        Wn[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y + lane4));
+        Wn[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z + lane4));
+        Wn[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w + lane4));
+      }
+      uint32_t V[4];
       transpose4(W, V);
       if (f4 == 0) {
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4, V[q], acc[q]);
         continue;
       }
-      // rows start at the flagged elements: bit i of fm <=> element i of the group
+      if ((f4 & (f4 - 1u)) == 0) {
+        // one row starts in this group, at byte i: bytes [0, i) end the open row
+        const uint32_t m = (f4 & (0u - f4)) - 1u;
+        const uint32_t lo = v4 & m, hi = v4 & ~m;
+        int32_t s[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) s[q] = dot4<SGN>(lo, V[q], acc[q]);
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(hi, V[q], 0);
+        if (owned) rows.finish(row, s);
+        if (closing) return;
+        row++;
+        owned = true;
+        continue;
+      }
+      // two or more rows start in this group: bit i of fm <=> element i starts a row
       uint32_t fm = (f4 * 0x01020408u) >> 24;
       uint32_t lo_mask = 0xFFFFFFFFu;  // bytes of the group not yet accumulated
       do {
@@ -232,14 +297,23 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
   const bool thr_in_smem = (MODE == MODE_FILTER) && batch_thr_in_smem(a.split);
   unsigned char* wsm_all = smem + (size_t)a.cols * kBatchQ +
                            (batch_thr_in_smem(a.split) ? (size_t)a.split * kBatchQ * 4 : 0);
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  // the warp index through a shuffle from lane 0: the compiler then treats the range bounds, and
+  // every branch on them, as warp-uniform
+  const uint32_t warp = __shfl_sync(0xFFFFFFFFu, threadIdx.x >> 5, 0), lane = threadIdx.x & 31u;
   unsigned char* wsm = wsm_all + (size_t)warp * batch_warp_bytes<B>();
+  if (lane < 4) {  // the zero group after the tile's records (never written by the decode)
+    constexpr uint32_t NR = batch_rec_elems<B>();
+    reinterpret_cast<uint32_t*>(wsm)[NR - 4 + lane] = 0u;
+    wsm[(size_t)NR * 4 + NR - 4 + lane] = 0u;
+    wsm[(size_t)NR * 5 + NR - 4 + lane] = 0u;
+  }
   {
     const uint4* src = reinterpret_cast<const uint4*>(a.qtab);
     uint4* dst = reinterpret_cast<uint4*>(qtb);
     for (uint32_t i = threadIdx.x; i < a.cols * (kBatchQ / 16); i += blockDim.x) dst[i] = src[i];
   }
-  BatchRows<MODE> rows{a, nullptr, {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, 0u, lane};
+  BatchRows<MODE> rows{a, nullptr, {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu},
+                       {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF}, 0u, lane};
   if constexpr (MODE == MODE_FILTER) {
     if (thr_in_smem) {
       for (uint32_t i = threadIdx.x; i < a.split * kBatchQ; i += blockDim.x) {
@@ -252,6 +326,7 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
       for (int t = 0; t < 4; t++) {
         const uint32_t q = 4 * lane + t;
         rows.thr4[t] = q < a.nq ? a.thr[(size_t)(a.q0 + q) * a.split] : 0xFFFFFFFFu;
+        rows.thr_sc[t] = (int32_t)(rows.thr4[t] ^ 0x80000000u);
       }
     }
   }
