@@ -315,7 +315,9 @@ __host__ __device__ constexpr size_t plain_stage_bytes() {
 template <int B, bool SGN, int MODE>
 __global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t warp = threadIdx.x >> 5;
+  // the warp index through a shuffle from lane 0, so the range bounds and every branch on them
+  // are known to be warp-uniform
+  const uint32_t warp = __shfl_sync(0xFFFFFFFFu, threadIdx.x >> 5, 0);
   const char* qtb = reinterpret_cast<const char*>(smem);            // int16 qt[cols][32]
   int16_t* qt = reinterpret_cast<int16_t*>(smem);
   uint4* E4all = reinterpret_cast<uint4*>(smem + (size_t)a.cols * 64);
