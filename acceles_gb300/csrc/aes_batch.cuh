@@ -184,6 +184,7 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
       return;
     }
     const bool closing = (t >= te);
+    bool simple = owned && !closing;  // boundaries need neither the ownership nor the end test
     // prefetch one tile ahead up to the first closing tile; later tiles are read on demand
     if (t + 1 <= te && t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
     // ---- phase A: this lane's packet -> records ----------------------------------------------
@@ -253,10 +254,16 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
         for (int q = 0; q < 4; q++) s[q] = dot4<SGN>(lo, V[q], acc[q]);
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(hi, V[q], 0);
+        if (simple) {  // an owned row inside the range
+          rows.finish(row, s);
+          row++;
+          continue;
+        }
         if (owned) rows.finish(row, s);
         if (closing) return;
         row++;
         owned = true;
+        simple = true;
         continue;
       }
       // two or more rows start in this group: bit i of fm <=> element i starts a row
@@ -276,6 +283,7 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
         for (int q = 0; q < 4; q++) acc[q] = 0;
         lo_mask = 0xFFFFFFFFu << (8 * i);
       } while (fm);
+      simple = true;  // owned now, and not closing (that returned above)
 #pragma unroll
       for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & lo_mask, V[q], acc[q]);
     }
