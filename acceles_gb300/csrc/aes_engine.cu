@@ -67,6 +67,12 @@ static PlainKernel pick_plain(int bits, bool sgn, int mode) {
   }
 }
 
+static uint32_t pow2_at_least(uint32_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
 // P(Bin(n, f) >= r) in log space
 static double binom_tail(uint32_t n, double f, uint32_t r) {
   if (r == 0) return 1.0;
@@ -440,7 +446,7 @@ int Engine::apply_config(const Config& c) {
   {
     uint32_t kp = 1;
     while (kp < p.k_max) kp <<= 1;
-    final_smem = ((cols * 4 + 15) & ~15u) + (size_t)std::max(npow2, kp) * 8;
+    final_smem = final_smem_bytes(cols, std::max(nslots, p.k_max), kp);
   }
   prm = p;
   cur = c;
@@ -528,19 +534,19 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   }
 
   // the shared-memory limit is an attribute of the kernel, shared by every handle: raise it to
-  // the device maximum once instead of to this handle's size
-  for (int mode = 0; mode < 3; mode++) {
-    PlainKernel kf = pick_plain((int)bits, sgn, mode);
-    AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                smem_optin));
-  }
-  for (int mode = 0; mode < 2; mode++) {
-    BatchKernel kf = pick_batch((int)bits, sgn, mode);
-    AES_CK(cudaFuncSetAttribute((const void*)kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                smem_optin));
-  }
-  AES_CK(cudaFuncSetAttribute((const void*)k_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              smem_optin));
+  // the device maximum (less the kernel's static shared memory) once, not to this handle's size
+  auto raise_smem = [&](const void* f) -> cudaError_t {
+    cudaFuncAttributes fa{};
+    cudaError_t e = cudaFuncGetAttributes(&fa, f);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                smem_optin - (int)fa.sharedSizeBytes);
+  };
+  for (int mode = 0; mode < 3; mode++)
+    AES_CK(raise_smem((const void*)pick_plain((int)bits, sgn, mode)));
+  for (int mode = 0; mode < 2; mode++)
+    AES_CK(raise_smem((const void*)pick_batch((int)bits, sgn, mode)));
+  AES_CK(raise_smem((const void*)k_final));
   rc = apply_config(c);
   if (rc) return rc;
   AES_CK(cudaDeviceSynchronize());
@@ -711,7 +717,7 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
       if (rc) return rc;
     }
   }
-  k_threshold<<<dim3(split, nq), 512, 0, s>>>(d_sample_keys, n_sample_rows, batched ? kBatchQ : 0,
+  k_threshold<<<dim3(split, nq), kThreadsThr, 0, s>>>(d_sample_keys, n_sample_rows, batched ? kBatchQ : 0,
                                               d_part_sample_begin, split, d_part_r, d_thr, d_cnt);
   AES_CK(cudaGetLastError());
   if (batched) {
@@ -748,12 +754,12 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   fa.cols = cols;
   fa.cand = d_cand;
   fa.nslots = nslots;
-  fa.npow2 = npow2;
+  fa.kp = pow2_at_least(k);
   fa.k = k;
   fa.out_idx = d_idx;
   fa.out_score = d_score;
   fa.status = d_status;
-  k_final<<<nq, 1024, final_smem, s>>>(fa);
+  k_final<<<nq, kThreadsFinal, final_smem, s>>>(fa);
   AES_CK(cudaGetLastError());
   return AES_OK;
 }
@@ -838,12 +844,12 @@ int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cud
     fa.cols = cols;
     fa.cand = d_cand + (size_t)q * nslots;
     fa.nslots = nslots;
-    fa.npow2 = npow2;
+    fa.kp = pow2_at_least(k);
     fa.k = k;
     fa.out_idx = d_idx + (size_t)q * k;
     fa.out_score = d_score + (size_t)q * k;
     fa.status = nullptr;
-    k_final<<<1, 1024, final_smem, s>>>(fa);
+    k_final<<<1, kThreadsFinal, final_smem, s>>>(fa);
     AES_CK(cudaGetLastError());
   }
   if (nrep) {
@@ -1153,12 +1159,12 @@ int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score
     fa.cols = e.cols;
     fa.cand = e.d_exact_cand;
     fa.nslots = k;
-    fa.npow2 = kp;
+    fa.kp = kp;
     fa.k = k;
     fa.out_idx = e.d_out_idx;
     fa.out_score = e.d_out_score;
     fa.status = nullptr;
-    k_final<<<1, 1024, e.final_smem, e.stream>>>(fa);
+    k_final<<<1, kThreadsFinal, e.final_smem, e.stream>>>(fa);
     AES_CK(cudaGetLastError());
     AES_CK(cudaEventRecord(e.ev1, e.stream));
     AES_CK(cudaMemcpyAsync(out_idx + (size_t)q * k, e.d_out_idx, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
@@ -1345,7 +1351,7 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
     return AES_OK;
   };
   if ((rc = plain(MODE_SAMPLE, skeys))) return rc;
-  k_threshold<<<dim3(e.split, 1), 512, 0, s>>>(skeys, e.n_sample_rows, 0, e.d_part_sample_begin,
+  k_threshold<<<dim3(e.split, 1), kThreadsThr, 0, s>>>(skeys, e.n_sample_rows, 0, e.d_part_sample_begin,
                                                e.split, e.d_part_r, thr, cnt);
   AES_CK(cudaGetLastError());
   if ((rc = plain(MODE_FILTER, nullptr))) return rc;
@@ -1371,12 +1377,12 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
   fa.cols = e.cols;
   fa.cand = cand;
   fa.nslots = e.nslots;
-  fa.npow2 = e.npow2;
+  fa.kp = aes::pow2_at_least(k);
   fa.k = k;
   fa.out_idx = d_idx;
   fa.out_score = d_score;
   fa.status = status;
-  k_final<<<1, 1024, e.final_smem, s>>>(fa);
+  k_final<<<1, kThreadsFinal, e.final_smem, s>>>(fa);
   AES_CK(cudaGetLastError());
   uint32_t st = 0;
   AES_CK(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s));
@@ -1391,7 +1397,7 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
     k_select<true><<<dim3(e.split, 1), 512, 0, s>>>(sa);
     AES_CK(cudaGetLastError());
     fa.status = nullptr;
-    k_final<<<1, 1024, e.final_smem, s>>>(fa);
+    k_final<<<1, kThreadsFinal, e.final_smem, s>>>(fa);
     AES_CK(cudaGetLastError());
     AES_CK(cudaStreamSynchronize(s));
   }

@@ -433,6 +433,8 @@ __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_
 // block helpers
 // ---------------------------------------------------------------------------------------------
 constexpr int kHistBins = 2048;
+constexpr int kThrILP = 4;  // keys in flight per thread in the threshold passes
+constexpr int kThreadsThr = 256;  // 80 registers: three CTAs per SM, a 256-query batch in one wave
 
 // Largest bin b with sum(hist[b..]) >= need; *above = sum(hist[b+1..]).  Executed by warp 0.
 __device__ __forceinline__ void warp_find_suffix_bin(const uint32_t* hist, int nbins,
@@ -507,11 +509,21 @@ __global__ void k_threshold(const uint32_t* __restrict__ keys_all, uint32_t ld_k
     if (threadIdx.x == 0) *T = 0;  // too few samples: keep every row of the partition
     return;
   }
+  // every pass reads kThrILP keys per thread before using them: the loops are bound by global
+  // load latency otherwise
   uint32_t mn = 0xFFFFFFFFu, mx = 0;
-  for (uint32_t i = a + threadIdx.x; i < b; i += blockDim.x) {
-    uint32_t v = kk[i];
-    mn = min(mn, v);
-    mx = max(mx, v);
+  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x * kThrILP) {
+    uint32_t v[kThrILP];
+#pragma unroll
+    for (int u = 0; u < kThrILP; u++) {
+      const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+      v[u] = i < b ? kk[i] : kk[a];
+    }
+#pragma unroll
+    for (int u = 0; u < kThrILP; u++) {
+      mn = min(mn, v[u]);
+      mx = max(mx, v[u]);
+    }
   }
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) {
@@ -543,13 +555,22 @@ __global__ void k_threshold(const uint32_t* __restrict__ keys_all, uint32_t ld_k
   const int sh1 = bl > 11 ? bl - 11 : 0;
   for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x) {
-    const uint32_t i = i0 + threadIdx.x;
-    const unsigned act = __ballot_sync(0xFFFFFFFFu, i < b);
-    if (i < b) {
-      const uint32_t bin = (kk[i] - mn) >> sh1;
-      const unsigned peers = __match_any_sync(act, bin);
-      if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x * kThrILP) {
+    uint32_t v[kThrILP];
+#pragma unroll
+    for (int u = 0; u < kThrILP; u++) {
+      const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+      v[u] = i < b ? kk[i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kThrILP; u++) {
+      const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+      const unsigned act = __ballot_sync(0xFFFFFFFFu, i < b);
+      if (i < b) {
+        const uint32_t bin = (v[u] - mn) >> sh1;
+        const unsigned peers = __match_any_sync(act, bin);
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+      }
     }
   }
   __syncthreads();
@@ -564,14 +585,23 @@ __global__ void k_threshold(const uint32_t* __restrict__ keys_all, uint32_t ld_k
   __syncthreads();
   for (int i = threadIdx.x; i < kHistBins; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x) {
-    const uint32_t i = i0 + threadIdx.x;
-    const bool in = (i < b) && (((kk[i] - mn) >> sh1) == b1);
-    const unsigned act = __ballot_sync(0xFFFFFFFFu, in);
-    if (in) {
-      const uint32_t bin = ((kk[i] - mn) >> sh2) & ((1u << (sh1 - sh2)) - 1u);
-      const unsigned peers = __match_any_sync(act, bin);
-      if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+  for (uint32_t i0 = a; i0 < b; i0 += blockDim.x * kThrILP) {
+    uint32_t v[kThrILP];
+#pragma unroll
+    for (int u = 0; u < kThrILP; u++) {
+      const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+      v[u] = i < b ? kk[i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kThrILP; u++) {
+      const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+      const bool in = (i < b) && (((v[u] - mn) >> sh1) == b1);
+      const unsigned act = __ballot_sync(0xFFFFFFFFu, in);
+      if (in) {
+        const uint32_t bin = ((v[u] - mn) >> sh2) & ((1u << (sh1 - sh2)) - 1u);
+        const unsigned peers = __match_any_sync(act, bin);
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+      }
     }
   }
   __syncthreads();
@@ -749,7 +779,8 @@ __global__ void k_select(SelectArgs a) {
 // ---------------------------------------------------------------------------------------------
 // k_final: FP32 rescoring of every candidate (sequential over the row's entries in column
 // order, separately rounded multiply and add) and the final Top-K in sort_tuples order.
-// One CTA per query; the candidate slots are sorted by a bitonic network in shared memory.
+// One CTA per query: the K largest (score, row) composites are found by a block radix select,
+// then only those are sorted by a bitonic network in shared memory.
 // ---------------------------------------------------------------------------------------------
 struct FinalArgs {
   const uint32_t* csr_ptr;   // [rows+1]
@@ -758,60 +789,83 @@ struct FinalArgs {
   const float* q32;          // [nq][ld32]
   uint32_t ld32, cols;
   const uint32_t* cand;      // [nq][nslots]
-  uint32_t nslots, npow2, k;
+  uint32_t nslots, kp, k;    // kp: power of two >= k
   uint32_t* out_idx;         // [nq][k]
   float* out_score;          // [nq][k]
   const uint32_t* status;    // [nq]; queries with a set status are left to the repair path
 };
 
-__global__ void __launch_bounds__(1024) k_final(FinalArgs a) {
+// dynamic shared memory of k_final: the query, the composites of all slots, the kp selected
+__host__ __device__ inline size_t final_smem_bytes(uint32_t cols, uint32_t nslots, uint32_t kp) {
+  return (((size_t)cols * 4 + 15) & ~(size_t)15) + (size_t)nslots * 8 + (size_t)kp * 8;
+}
+
+constexpr int kThreadsFinal = 512;  // two CTAs per SM: a 256-query batch runs in one wave
+
+__global__ void __launch_bounds__(kThreadsFinal, 2) k_final(FinalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t hist[256];
+  __shared__ uint64_t sh64[72];
+  __shared__ uint32_t s_cnt;
   float* qs = reinterpret_cast<float*>(smem);
   uint64_t* comp = reinterpret_cast<uint64_t*>(smem + ((a.cols * 4 + 15) & ~15u));
+  uint64_t* top = comp + a.nslots;
   const uint32_t q = blockIdx.x;
   if (a.status && a.status[q]) return;
   const float* x = a.q32 + (size_t)q * a.ld32;
   for (uint32_t j = threadIdx.x; j < a.cols; j += blockDim.x) qs[j] = x[j];
+  for (uint32_t i = threadIdx.x; i < a.kp; i += blockDim.x) top[i] = 0;
+  if (threadIdx.x == 0) s_cnt = 0;
   __syncthreads();
   const uint32_t* cr = a.cand + (size_t)q * a.nslots;
-  for (uint32_t i = threadIdx.x; i < a.npow2; i += blockDim.x) {
+  for (uint32_t i = threadIdx.x; i < a.nslots; i += blockDim.x) {
     uint64_t c = 0;
-    if (i < a.nslots) {
-      uint32_t row = cr[i];
-      if (row != 0xFFFFFFFFu) {
-        uint32_t e = a.csr_ptr[row], e1 = a.csr_ptr[row + 1];
-        float acc = 0.0f;
-        for (; e + 4 <= e1; e += 4) {
-          uint16_t c0 = a.csr_col[e], c1 = a.csr_col[e + 1], c2 = a.csr_col[e + 2], c3 = a.csr_col[e + 3];
-          float v0 = a.csr_val[e], v1 = a.csr_val[e + 1], v2 = a.csr_val[e + 2], v3 = a.csr_val[e + 3];
-          acc = __fadd_rn(acc, __fmul_rn(v0, qs[c0]));
-          acc = __fadd_rn(acc, __fmul_rn(v1, qs[c1]));
-          acc = __fadd_rn(acc, __fmul_rn(v2, qs[c2]));
-          acc = __fadd_rn(acc, __fmul_rn(v3, qs[c3]));
-        }
-        for (; e < e1; e++) acc = __fadd_rn(acc, __fmul_rn(a.csr_val[e], qs[a.csr_col[e]]));
-        c = ((uint64_t)key_f32(acc) << 32) | row;
+    const uint32_t row = cr[i];
+    if (row != 0xFFFFFFFFu) {
+      uint32_t e = a.csr_ptr[row], e1 = a.csr_ptr[row + 1];
+      float acc = 0.0f;
+      for (; e + 4 <= e1; e += 4) {
+        uint16_t c0 = a.csr_col[e], c1 = a.csr_col[e + 1], c2 = a.csr_col[e + 2], c3 = a.csr_col[e + 3];
+        float v0 = a.csr_val[e], v1 = a.csr_val[e + 1], v2 = a.csr_val[e + 2], v3 = a.csr_val[e + 3];
+        acc = __fadd_rn(acc, __fmul_rn(v0, qs[c0]));
+        acc = __fadd_rn(acc, __fmul_rn(v1, qs[c1]));
+        acc = __fadd_rn(acc, __fmul_rn(v2, qs[c2]));
+        acc = __fadd_rn(acc, __fmul_rn(v3, qs[c3]));
       }
+      for (; e < e1; e++) acc = __fadd_rn(acc, __fmul_rn(a.csr_val[e], qs[a.csr_col[e]]));
+      c = ((uint64_t)key_f32(acc) << 32) | row;
     }
     comp[i] = c;
   }
   __syncthreads();
-  // bitonic sort, descending
-  for (uint32_t kk = 2; kk <= a.npow2; kk <<= 1) {
+  // composites of filled slots are unique (rows are); empty slots are 0 and never selected
+  const uint32_t need = min(a.k, a.nslots);
+  const uint64_t tau = block_select_tau([&](uint32_t i) -> uint64_t { return comp[i]; }, a.nslots,
+                                        need, hist, sh64);
+  for (uint32_t i = threadIdx.x; i < a.nslots; i += blockDim.x) {
+    const uint64_t c = comp[i];
+    if (c != 0 && c >= tau) {
+      const uint32_t o = atomicAdd(&s_cnt, 1u);
+      if (o < a.kp) top[o] = c;
+    }
+  }
+  __syncthreads();
+  // bitonic sort of the kp selected composites, descending
+  for (uint32_t kk = 2; kk <= a.kp; kk <<= 1) {
     for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
-      for (uint32_t i = threadIdx.x; i < a.npow2; i += blockDim.x) {
+      for (uint32_t i = threadIdx.x; i < a.kp; i += blockDim.x) {
         uint32_t l = i ^ j;
         if (l > i) {
-          uint64_t ci = comp[i], cl = comp[l];
+          uint64_t ci = top[i], cl = top[l];
           bool desc = ((i & kk) == 0);
-          if (desc ? (ci < cl) : (ci > cl)) { comp[i] = cl; comp[l] = ci; }
+          if (desc ? (ci < cl) : (ci > cl)) { top[i] = cl; top[l] = ci; }
         }
       }
       __syncthreads();
     }
   }
   for (uint32_t i = threadIdx.x; i < a.k; i += blockDim.x) {
-    uint64_t c = (i < a.npow2) ? comp[i] : 0;
+    uint64_t c = (i < a.kp) ? top[i] : 0;
     uint32_t* oi = a.out_idx + (size_t)q * a.k;
     float* os = a.out_score + (size_t)q * a.k;
     if (c == 0) {

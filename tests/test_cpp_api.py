@@ -29,7 +29,9 @@ def test_cpp_wrapper_compiles_and_links():
 
 @pytest.mark.gpu
 def test_cpp_wrapper_matches_oracle():
-    out = subprocess.run([build_exe(), "7"], capture_output=True, text=True, check=True).stdout
+    res = subprocess.run([build_exe(), "7"], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    out = res.stdout
     lines = {l.split(" ", 1)[0]: l.split(" ", 1)[1] for l in out.strip().splitlines()}
     q = np.array([float(v) for v in lines["query"].split()], np.float32)
     cand = [tuple(t.split(":")) for t in lines["cand"].split()]
