@@ -433,7 +433,7 @@ __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_
 // block helpers
 // ---------------------------------------------------------------------------------------------
 constexpr int kHistBins = 2048;
-constexpr int kThrILP = 4;  // keys in flight per thread in the threshold passes
+constexpr int kThrILP = 8;  // keys in flight per thread in the threshold passes
 constexpr int kThreadsThr = 256;  // 80 registers: three CTAs per SM, a 256-query batch in one wave
 
 // Largest bin b with sum(hist[b..]) >= need; *above = sum(hist[b+1..]).  Executed by warp 0.
