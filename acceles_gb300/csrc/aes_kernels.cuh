@@ -100,6 +100,16 @@ struct Emitter {
   const uint32_t* thr_s;  // shared copy of the thresholds (split > 1)
   uint32_t thr0;          // threshold when split == 1
   uint32_t sample_base;   // MODE_SAMPLE: first owned row minus its key index
+  // filter with integer keys and one partition: key >= thr0 <=> score >= thr0 ^ 0x80000000
+  __device__ __forceinline__ bool int_filter() const {
+    return MODE == MODE_FILTER && !a.rowscale && a.split <= 1;
+  }
+  __device__ __forceinline__ int32_t thr_score() const { return (int32_t)(thr0 ^ 0x80000000u); }
+  // a row of the integer filter whose score passed thr_score()
+  __device__ __forceinline__ void append_int(uint32_t row, int32_t score) const {
+    const uint32_t i = atomicAdd(a.cnt, 1u);
+    if (i < a.cap) a.surv[i] = make_uint2(key_i32(score), row);
+  }
   __device__ __forceinline__ void operator()(uint32_t row, int32_t score) const {
     uint32_t key;
     if (a.rowscale) key = key_f32(__fmul_rn(__int2float_rn(score), __ldg(a.rowscale + row)));
@@ -261,13 +271,28 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
     f &= f - 1;
     row++;
   }
-  while (f) {  // each flag closes the row before it
-    const int j = ffs_flags(f);
-    f &= f - 1;
-    const uint32_t Gb = LB + prefix_before(Ew, lane, j);
-    emit(row, (int32_t)(Gb - prevG));
-    prevG = Gb;
-    row++;
+  if (emit.int_filter()) {
+    // the common case, chosen once outside the per-lane loop: a compare per row, and the
+    // survivor append only on a hit
+    const int32_t ts = emit.thr_score();
+    while (f) {  // each flag closes the row before it
+      const int j = ffs_flags(f);
+      f &= f - 1;
+      const uint32_t Gb = LB + prefix_before(Ew, lane, j);
+      const int32_t sc = (int32_t)(Gb - prevG);
+      if (sc >= ts) emit.append_int(row, sc);
+      prevG = Gb;
+      row++;
+    }
+  } else {
+    while (f) {  // each flag closes the row before it
+      const int j = ffs_flags(f);
+      f &= f - 1;
+      const uint32_t Gb = LB + prefix_before(Ew, lane, j);
+      emit(row, (int32_t)(Gb - prevG));
+      prevG = Gb;
+      row++;
+    }
   }
   if (has_mask) {
     st.startG = __shfl_sync(0xFFFFFFFFu, lastGb, 31 - __clz(has_mask));
