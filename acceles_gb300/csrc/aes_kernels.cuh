@@ -155,23 +155,34 @@ __device__ __forceinline__ uint32_t window32(const uint32_t (&w)[16]) {
 }
 
 // Per-lane decode of one packet.  Element j: 10-bit column at bit P + 10j, B-bit value at bit
-// 11P + Bj (fpga_utils.hpp:349-384).  Running prefix S_j = sum_{i<=j} val_i * q[col_i] (int32,
-// wrapping) is staged four at a time in E4[(j/4)*32 + lane]; returns S_{P-1}.
+// 11P + Bj (fpga_utils.hpp:349-384).  run() returns the packet's sum of val_i * q[col_i]
+// (int32, wrapping) and stages what prefix() needs to give the running sum before any entry:
+//  - B = 8: four consecutive values are one 32-bit window, so each group of four entries is
+//    one dp4a of the packed values with the four query bytes; a group stages (sum before the
+//    group, values, query bytes) and prefix() finishes with a masked dp4a;
+//  - B = 4, 6: the running sum S_j of every entry, four per 16-byte slot.
 template <int B, bool SGN>
 struct PacketDecoder {
   static constexpr int P = packet_elems(B);
   static constexpr int NG = (P + 3) / 4;
+  static constexpr bool kGroups = (B == 8);
   using Flags = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
+
+  // q[col_J] from the lane-replicated table qt[col][32] (int16): the column window starts 6
+  // bits early so (col << 6), the row offset of col in the table, lands at bits 6..15
+  template <int J>
+  __device__ __forceinline__ static int32_t qval(const uint32_t (&w)[16], const char* qtb,
+                                                 uint32_t lane2) {
+    const uint32_t y = window32<P + 10 * J - 6>(w);
+    return *reinterpret_cast<const int16_t*>(qtb + ((y & 0xFFC0u) | lane2));
+  }
 
   template <int J>
   __device__ __forceinline__ static void step(const uint32_t (&w)[16], const char* qtb,
                                               uint32_t lane2, uint4* E4, int32_t& S,
                                               int32_t (&s4)[4]) {
     if constexpr (J < P) {
-      // column window starting 6 bits early: (col << 6) lands at bits 6..15, the byte offset
-      // of q[col] in the lane-replicated table qt[col][32] (int16)
-      const uint32_t y = window32<P + 10 * J - 6>(w);
-      const int32_t q = *reinterpret_cast<const int16_t*>(qtb + ((y & 0xFFC0u) | lane2));
+      const int32_t q = qval<J>(w, qtb, lane2);
       const uint32_t z = window32<11 * P + B * J + B - 32>(w);  // value in the top B bits
       const int32_t v = SGN ? ((int32_t)z >> (32 - B)) : (int32_t)(z >> (32 - B));
       S += v * q;
@@ -181,13 +192,54 @@ struct PacketDecoder {
       step<J + 1>(w, qtb, lane2, E4, S, s4);
     }
   }
+
+  template <int G>
+  __device__ __forceinline__ static void group(const uint32_t (&w)[16], const char* qtb,
+                                               uint32_t lane2, uint4* E4, int32_t& S) {
+    if constexpr (G < NG) {
+      constexpr int J = 4 * G;
+      constexpr int n = (P - J) < 4 ? (P - J) : 4;  // entries in this group
+      const int32_t q0 = qval<J>(w, qtb, lane2);
+      const int32_t q1 = n > 1 ? qval<(n > 1 ? J + 1 : J)>(w, qtb, lane2) : 0;
+      const int32_t q2 = n > 2 ? qval<(n > 2 ? J + 2 : J)>(w, qtb, lane2) : 0;
+      const int32_t q3 = n > 3 ? qval<(n > 3 ? J + 3 : J)>(w, qtb, lane2) : 0;
+      const uint32_t q4 = __byte_perm(__byte_perm((uint32_t)q0, (uint32_t)q1, 0x0040),
+                                      __byte_perm((uint32_t)q2, (uint32_t)q3, 0x0040), 0x5410);
+      uint32_t v4 = window32<11 * P + 32 * G>(w);
+      if constexpr (n < 4) v4 &= (1u << (8 * n)) - 1u;
+      const int32_t Sb = S;
+      S = SGN ? __dp4a((int)v4, (int)q4, S) : (int32_t)__dp4a(v4, q4, (unsigned)S);
+      E4[G * 32] = make_uint4((uint32_t)Sb, v4, q4, 0u);
+      group<G + 1>(w, qtb, lane2, E4, S);
+    }
+  }
+
   __device__ __forceinline__ static int32_t run(const uint32_t (&w)[16], const char* qtb,
                                                 uint32_t lane2, uint4* E4) {
     int32_t S = 0;
-    int32_t s4[4] = {0, 0, 0, 0};
-    step<0>(w, qtb, lane2, E4, S, s4);
+    if constexpr (kGroups) {
+      group<0>(w, qtb, lane2, E4, S);
+    } else {
+      int32_t s4[4] = {0, 0, 0, 0};
+      step<0>(w, qtb, lane2, E4, S, s4);
+    }
     return S;
   }
+
+  // running sum of this lane's packet before entry j (0 for j == 0)
+  __device__ __forceinline__ static uint32_t prefix(const uint32_t* Ew, uint32_t lane, int j) {
+    if constexpr (kGroups) {
+      const uint4 g = reinterpret_cast<const uint4*>(Ew)[(j >> 2) * 32 + lane];
+      const uint32_t m = (1u << (8 * (j & 3))) - 1u;  // bytes of the group before entry j
+      return SGN ? (uint32_t)__dp4a((int)(g.y & m), (int)g.z, (int)g.x)
+                 : __dp4a(g.y & m, g.z, g.x);
+    } else {
+      if (j == 0) return 0u;
+      const int i = j - 1;
+      return Ew[(((i >> 2) * 32 + lane) << 2) | (i & 3)];
+    }
+  }
+
   __device__ __forceinline__ static Flags flags(const uint32_t (&w)[16]) {
     if constexpr (P <= 32) {
       return w[0] & ((P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u));
@@ -219,13 +271,6 @@ struct RangeState {
   uint32_t carryG;  // running sum before the current tile
 };
 
-// S_{j-1} of this lane's packet (0 for j == 0)
-__device__ __forceinline__ uint32_t prefix_before(const uint32_t* Ew, uint32_t lane, int j) {
-  if (j == 0) return 0u;
-  const int i = j - 1;
-  return Ew[(((i >> 2) * 32 + lane) << 2) | (i & 3)];
-}
-
 // One tile of a warp's range.  Returns true once the range is complete.
 template <int B, bool SGN, int MODE>
 __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32_t te,
@@ -252,7 +297,7 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
       return false;
     }
     if (lane == (uint32_t)(__ffs(has_mask) - 1)) {
-      const uint32_t Gb = LB + prefix_before(Ew, lane, ffs_flags(F));
+      const uint32_t Gb = LB + D::prefix(Ew, lane, ffs_flags(F));
       if (st.open_owned) emit(rowbase, (int32_t)(Gb - st.startG));
     }
     return true;
@@ -260,14 +305,14 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
   const uint32_t nf = popc_flags(F);
   const uint32_t rbase = rowbase + warp_incl_sum(nf, lane) - nf;
   uint32_t lastGb = 0;
-  if (F) lastGb = LB + prefix_before(Ew, lane, fls_flags(F));
+  if (F) lastGb = LB + D::prefix(Ew, lane, fls_flags(F));
   const uint32_t left = has_mask & ((1u << lane) - 1u);
   const uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, left ? (31 - __clz(left)) : 0u);
   uint32_t prevG = left ? inhG : st.startG;
   Flags f = F;
   uint32_t row = rbase;
   if (f && !left && !st.open_owned) {  // first flag closes a row started before the range
-    prevG = LB + prefix_before(Ew, lane, ffs_flags(f));
+    prevG = LB + D::prefix(Ew, lane, ffs_flags(f));
     f &= f - 1;
     row++;
   }
@@ -278,7 +323,7 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
     while (f) {  // each flag closes the row before it
       const int j = ffs_flags(f);
       f &= f - 1;
-      const uint32_t Gb = LB + prefix_before(Ew, lane, j);
+      const uint32_t Gb = LB + D::prefix(Ew, lane, j);
       const int32_t sc = (int32_t)(Gb - prevG);
       if (sc >= ts) emit.append_int(row, sc);
       prevG = Gb;
@@ -288,7 +333,7 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
     while (f) {  // each flag closes the row before it
       const int j = ffs_flags(f);
       f &= f - 1;
-      const uint32_t Gb = LB + prefix_before(Ew, lane, j);
+      const uint32_t Gb = LB + D::prefix(Ew, lane, j);
       emit(row, (int32_t)(Gb - prevG));
       prevG = Gb;
       row++;
