@@ -324,6 +324,8 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_cand_batch<8,signed,FILTER> (128 queries per pass)",
+                         "limiter": "CUDA-core integer issue (gathers, byte transposes, dp4a); "
+                                    "one matrix read serves 128 queries",
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": cand_ms},
             "plain_roofline": {"bound": "hbm", "achieved": plain_achieved, "peak": peak,
                                "unit": "GB/s", "frac": plain_achieved / peak,

@@ -247,3 +247,26 @@ def test_fp32_only_exact_path():
         s = orc.rescore_f32(m.ptr, m.col, m.val, Q[i], allrows)
         ri, rs = orc.sort_tuples_f32(allrows, s)
         assert np.array_equal(idx[i], ri[:k]) and np.array_equal(sc[i], rs[:k])
+
+
+@pytest.mark.parametrize("bits,quant,split,ck,k,nq", [(8, 0, 1, 4096, 1024, 3), (8, 1, 32, 2048, 1000, 20),
+                                                      (4, 2, 8, 1024, 777, 17)])
+def test_large_k_and_ck(bits, quant, split, ck, k, nq):
+    # the final pass selects the K best of up to 4096 rescored candidates, then sorts only those
+    rows, cols = 30000, 1024
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 31, bits, quant, split, ck, k, nq=nq)
+    Q = queries(cols, nq, 4, signed=(quant == 0))
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    for i in range(nq):
+        oi, os_, _ = m.two_stage(Q[i], split, ck, k)
+        assert np.array_equal(idx[i, :len(oi)], oi), f"query {i}"
+        assert np.array_equal(sc[i, :len(oi)], os_), f"query {i}"
+    # FP32-only path with the same K
+    ei, es, _ = eng.run_exact(k=k)
+    for i in range(nq):
+        s = orc.rescore_f32(m.ptr, m.col, m.val, Q[i], np.arange(rows, dtype=np.uint32))
+        s = np.where(s == 0, np.float32(0), s)
+        top = np.lexsort((-np.arange(rows, dtype=np.int64), -s.astype(np.float64)))[:k]
+        assert np.array_equal(ei[i], top.astype(np.uint32)), f"exact query {i}"
