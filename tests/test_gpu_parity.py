@@ -250,7 +250,8 @@ def test_fp32_only_exact_path():
 
 
 @pytest.mark.parametrize("bits,quant,split,ck,k,nq", [(8, 0, 1, 4096, 1024, 3), (8, 1, 32, 2048, 1000, 20),
-                                                      (4, 2, 8, 1024, 777, 17)])
+                                                      (4, 2, 8, 1024, 777, 17),
+                                                      (6, 0, 64, 2048, 100, 20)])
 def test_large_k_and_ck(bits, quant, split, ck, k, nq):
     # the final pass selects the K best of up to 4096 rescored candidates, then sorts only those
     rows, cols = 30000, 1024

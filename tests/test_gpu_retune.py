@@ -100,3 +100,27 @@ def test_autotune_reaches_target_and_leaves_handle_tuned():
     trials = [t for t in res["ck_trials"] if t["split"] == prm["split"]]
     assert trials[-1]["ck"] == prm["ck"] and trials[-1]["frac_identical"] == 1.0
     assert all(t["frac_identical"] < 1.0 for t in trials[:-1])
+
+
+def test_retune_drops_captured_graphs():
+    """A handle that replays CUDA graphs re-captures after a retune (the old graphs point at
+    freed buffers) and gives the fresh handle's results."""
+    rows, cols, k = 25000, 1024, 64
+    ptr, col, val, m = _setup(rows, cols)
+    Q = _queries(cols, 24, 12)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=1, ck=512,
+                 k_max=k, max_batch=24, flags=E.FLAG_GRAPHS)
+    for _ in range(2):  # capture, then replay
+        eng.Q_reset(Q)
+        eng(k=k)
+    eng.retune(ck=256, split=8, sample_stride=16)
+    for _ in range(2):
+        eng.Q_reset(Q)
+        eng(k=k)
+    idx, sc = eng.read_topk()
+    fresh = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=8, ck=256,
+                   k_max=k, max_batch=24, sample_stride=16)
+    fresh.Q_reset(Q)
+    fresh(k=k)
+    fi, fs = fresh.read_topk()
+    assert np.array_equal(idx, fi) and np.array_equal(sc, fs)
