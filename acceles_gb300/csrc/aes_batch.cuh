@@ -318,7 +318,21 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
   {
     const uint4* src = reinterpret_cast<const uint4*>(a.qtab);
     uint4* dst = reinterpret_cast<uint4*>(qtb);
-    for (uint32_t i = threadIdx.x; i < a.cols * (kBatchQ / 16); i += blockDim.x) dst[i] = src[i];
+    // eight independent loads per thread in flight: the fill is latency-bound otherwise
+    const uint32_t n = a.cols * (kBatchQ / 16);
+    for (uint32_t i0 = 0; i0 < n; i0 += 8 * blockDim.x) {
+      uint4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+        if (i < n) v[u] = src[i];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
+        if (i < n) dst[i] = v[u];
+      }
+    }
   }
   BatchRows<MODE> rows{a, nullptr, {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu},
                        {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF}, 0u, lane};
