@@ -109,7 +109,7 @@ struct Engine {
   // ---- configuration: selection geometry and per-batch buffers (aes_retune may change these) --
   struct Config {
     aes_params p{};
-    uint32_t split = 1, slice = 0, ntop = 0, nslots = 0, npow2 = 0, ck_eff = 0, cap = 0;
+    uint32_t split = 1, slice = 0, ntop = 0, nslots = 0, ck_eff = 0, cap = 0;
     uint32_t ss = 1, n_sample_tiles = 0, n_sample_rows = 0, maxB = 1;
     std::vector<uint32_t> sample_first, part_begin, part_r;
     size_t plan = 0;  // device bytes of the configuration's buffers
@@ -122,7 +122,7 @@ struct Engine {
   uint32_t* d_part_sample_begin = nullptr;
   uint32_t* d_part_r = nullptr;
 
-  uint32_t split = 1, slice = 0, ntop = 0, nslots = 0, npow2 = 0, ck_eff = 0, cap = 0;
+  uint32_t split = 1, slice = 0, ntop = 0, nslots = 0, ck_eff = 0, cap = 0;
 
   uint32_t maxB = 1, ld32 = 0, ld8 = 0;
   float* d_q32 = nullptr;
@@ -291,8 +291,6 @@ int Engine::plan_config(const aes_params& p, Config* c) const {
   c->slice = rows / S;
   c->ntop = p.ck / S;
   c->nslots = S * c->ntop;
-  c->npow2 = 1;
-  while (c->npow2 < c->nslots) c->npow2 <<= 1;
   c->ck_eff = 0;
   std::vector<uint32_t> prow(S);
   for (uint32_t q = 0; q < S; q++) {
@@ -384,7 +382,6 @@ int Engine::apply_config(const Config& c) {
   slice = c.slice;
   ntop = c.ntop;
   nslots = c.nslots;
-  npow2 = c.npow2;
   ck_eff = c.ck_eff;
   cap = c.cap;
   ss = c.ss;
