@@ -113,15 +113,30 @@ def make_queries(n, seed=SEED + 1):
     return np.random.default_rng(seed).random((n, COLS)).astype(np.float32)
 
 
-def cpu_baseline(ptr, col, val, queries, seconds, threads):
+def cpu_baseline(ptr, col, val, queries, seconds, threads, legs=True):
+    """The reference's CPU method (oracle port) on this host: the two-stage method on all
+    threads (the reported baseline) and, when `legs`, the two-stage method on one thread and
+    the FP32 full Top-K on one and on all threads, each a bounded sample."""
     import oracle as orc
     m = orc.Matrix(len(ptr) - 1, COLS, ptr, col, val, BITS, orc.QUANT_SYM_GLOBAL)
     el, done, _ = orc.bench_two_stage(m, queries, CK, K, nthreads=threads, max_seconds=seconds)
-    return m, {"value": done / el, "unit": "queries/s", "cores": threads, "kind": "port",
-               "sample": f"{done} queries of the same 10M x 1024 workload: two-stage method "
-                         f"(streaming Top-{CK} per row block as gold_algorithms.hpp:249-308, "
-                         f"merge, FP32 rescoring, sort_tuples), {threads} threads, "
-                         f"{el:.1f} s"}
+    cb = {"value": done / el, "unit": "queries/s", "cores": threads, "kind": "port",
+          "sample": f"{done} queries of the same 10M x 1024 workload: two-stage method "
+                    f"(streaming Top-{CK} per row block as gold_algorithms.hpp:249-308, "
+                    f"merge, FP32 rescoring, sort_tuples), {threads} threads, {el:.1f} s"}
+    if legs:
+        short = max(2.0, seconds / 3)
+        el1, d1, _ = orc.bench_two_stage(m, queries, CK, K, nthreads=1, max_seconds=short)
+        ef, df = orc.bench_fp32_topk(m, queries, K, nthreads=threads, max_seconds=short)
+        ef1, df1 = orc.bench_fp32_topk(m, queries, K, nthreads=1, max_seconds=short)
+        cb["legs"] = {
+            "two_stage_1_thread": {"queries_per_s": d1 / el1, "queries": d1},
+            "fp32_full_topk_threads": {"queries_per_s": df / ef, "queries": df, "threads": threads},
+            "fp32_full_topk_1_thread": {"queries_per_s": df1 / ef1, "queries": df1},
+            "note": "FP32 full Top-K = spmv_coo_gold_top_k (gold_algorithms.hpp:189-247) "
+                    "restated; threads = one row block per host thread, merged",
+        }
+    return m, cb
 
 
 def run_reference(args, rank, world):
@@ -132,7 +147,7 @@ def run_reference(args, rank, world):
     threads = os.cpu_count() or 1
     ptr, col, val = make_matrix()
     Q = make_queries(max(64, args.cpu_queries))
-    _, cb = cpu_baseline(ptr, col, val, Q, args.cpu_seconds, threads)
+    _, cb = cpu_baseline(ptr, col, val, Q, args.cpu_seconds, threads, legs=False)
     line = {"metric": METRIC, "value": cb["value"], "unit": "queries/s", "impl": "reference",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",

@@ -575,6 +575,78 @@ double orc_bench_two_stage(const uint64_t* ptr, const uint32_t* col, const float
   return el;
 }
 
+typedef struct {
+  const uint64_t* ptr;
+  const uint32_t* col;
+  const float* val;
+  const float* q;
+  uint32_t r0, r1;
+  int k;
+  uint32_t* idx;
+  float* out;
+} orc_fjob_t;
+
+/* streaming FP32 Top-k of gold_algorithms.hpp:189-247 over the rows [r0, r1) of a CSR (the
+ * reference walks a row-sorted COO; the rows and their entry order are the same) */
+static void* orc_fjob_run(void* arg) {
+  orc_fjob_t* j = (orc_fjob_t*)arg;
+  for (int i = 0; i < j->k; i++) { j->idx[i] = 0; j->out[i] = 0.0f; }
+  int wi = 0;
+  float wv = 0.0f;
+  for (uint32_t r = j->r0; r < j->r1; r++) {
+    float s = 0.0f;
+    for (uint64_t e = j->ptr[r]; e < j->ptr[r + 1]; e++) s = s + j->val[e] * j->q[j->col[e]];
+    if (s >= wv) {
+      j->idx[wi] = r;
+      j->out[wi] = s;
+      int bi = 0;
+      float bv = j->out[0];
+      for (int t = 0; t < j->k; t++)
+        if (j->out[t] < bv) { bi = t; bv = j->out[t]; }
+      wi = bi;
+      wv = bv;
+    }
+  }
+  return NULL;
+}
+
+double orc_bench_fp32_topk(const uint64_t* ptr, const uint32_t* col, const float* val,
+                           uint32_t rows, uint32_t cols, uint32_t k, const float* queries,
+                           uint32_t nq, int nthreads, double max_seconds, uint32_t* done) {
+  if (nthreads < 1) nthreads = 1;
+  orc_fjob_t* jobs = (orc_fjob_t*)malloc(sizeof(orc_fjob_t) * nthreads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+  uint32_t* cidx = (uint32_t*)malloc(sizeof(uint32_t) * k * nthreads);
+  float* cval = (float*)malloc(sizeof(float) * k * nthreads);
+  comp_t* cc = (comp_t*)malloc(sizeof(comp_t) * k * nthreads);
+  double t0 = orc_now();
+  uint32_t n = 0;
+  for (; n < nq; n++) {
+    if (n > 0 && orc_now() - t0 > max_seconds) break;
+    const float* x = queries + (size_t)n * cols;
+    for (int t = 0; t < nthreads; t++) {
+      jobs[t].ptr = ptr; jobs[t].col = col; jobs[t].val = val; jobs[t].q = x;
+      jobs[t].r0 = (uint32_t)((uint64_t)rows * t / nthreads);
+      jobs[t].r1 = (uint32_t)((uint64_t)rows * (t + 1) / nthreads);
+      jobs[t].k = (int)k;
+      jobs[t].idx = cidx + (size_t)t * k;
+      jobs[t].out = cval + (size_t)t * k;
+      if (nthreads == 1) orc_fjob_run(&jobs[t]);
+      else pthread_create(&th[t], NULL, orc_fjob_run, &jobs[t]);
+    }
+    if (nthreads > 1)
+      for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    uint32_t m = k * (uint32_t)nthreads;
+    for (uint32_t i = 0; i < m; i++)
+      cc[i].comp = ((uint64_t)orc_key_f32(cval[i]) << 32) | cidx[i];
+    qsort(cc, m, sizeof(comp_t), cmp_comp_desc);  /* the blocks' Top-k merged */
+  }
+  double el = orc_now() - t0;
+  *done = n;
+  free(jobs); free(th); free(cidx); free(cval); free(cc);
+  return el;
+}
+
 /* ---------------------------------------------------------------------------------------- */
 /* ReSparse (quantify_util.py:375-403)                                                        */
 /* ---------------------------------------------------------------------------------------- */

@@ -137,6 +137,13 @@ double orc_bench_two_stage(const uint64_t* ptr, const uint32_t* col, const float
                            const float* queries, uint32_t nq, int nthreads, double max_seconds,
                            uint32_t* done, uint32_t* out_idx);
 
+/* FP32 full Top-K timing (spmv_coo_gold_top_k, gold_algorithms.hpp:189-247, V = float): each of
+ * nthreads threads runs the streaming Top-k over its row block, then the blocks' results merge by
+ * (score desc, row desc).  Same stopping rule and return value as orc_bench_two_stage. */
+double orc_bench_fp32_topk(const uint64_t* ptr, const uint32_t* col, const float* val,
+                           uint32_t rows, uint32_t cols, uint32_t k, const float* queries,
+                           uint32_t nq, int nthreads, double max_seconds, uint32_t* done);
+
 /* ReSparse per-row pruning, restating resparse_spm (quantify_util.py:375-403) on a CSR sorted by
  * (row, col) without duplicates: mean |v| over rows x cols (zeros included, plain double sum in
  * entry order); a row whose smallest nonzero |v| exceeds the mean is kept whole, else its

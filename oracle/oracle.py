@@ -122,6 +122,10 @@ def lib():
                                           ctypes.c_uint32, ctypes.c_uint32, _f32p,
                                           ctypes.c_uint32, ctypes.c_int, ctypes.c_double, _u32p,
                                           _u32p]
+        L.orc_bench_fp32_topk.restype = ctypes.c_double
+        L.orc_bench_fp32_topk.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_uint32, _f32p, ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.c_double, _u32p]
         L.orc_resparse.restype = ctypes.c_uint64
         L.orc_resparse.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_double, _u64p, _u32p, _f32p]
@@ -363,6 +367,17 @@ def bench_two_stage(m: "Matrix", queries, ck, k, nthreads=1, max_seconds=10.0):
                                    m.rows, m.cols, m.bits, ck, k, _p(Q, _f32p), Q.shape[0],
                                    nthreads, max_seconds, _p(done, _u32p), _p(out, _u32p))
     return el, int(done[0]), out[: int(done[0])]
+
+
+def bench_fp32_topk(m: "Matrix", queries, k, nthreads=1, max_seconds=10.0):
+    """Time the CPU FP32 full Top-K (spmv_coo_gold_top_k) on host threads.
+    Returns (seconds, queries done)."""
+    Q = np.ascontiguousarray(queries, np.float32)
+    done = np.zeros(1, np.uint32)
+    el = lib().orc_bench_fp32_topk(_p(m.ptr, _u64p), _p(m.col, _u32p), _p(m.val, _f32p),
+                                   m.rows, m.cols, k, _p(Q, _f32p), Q.shape[0], nthreads,
+                                   max_seconds, _p(done, _u32p))
+    return el, int(done[0])
 
 
 # ---------------------------------------------------------------------------------------------
