@@ -2,7 +2,7 @@
 //
 // Stages (reference: zhaijiaqi/AccelES):
 //   k_quantize        quantify_vector (quantify_util.py:31-49) / quantize_vec
-//                     (quantize_utils.hpp:8-18), float64 arithmetic, one CTA per query
+//                     (quantize_utils.hpp:8-18): float64 results in integer arithmetic, one CTA per query
 //   k_cand_plain      the low-bit candidate pass of spmv_ucsr_top_k_main
 //                     (spmv_ucsr_top_k_multicore.hpp:195-413; CPU gold spmv_coo_gold_top_k_2,
 //                     gold_algorithms.hpp:249-308): streams Ultra-CSR tiles, decodes flags,
@@ -18,6 +18,8 @@
 #include <stdint.h>
 
 #include <type_traits>
+
+#include "aes_qexact.hpp"
 
 namespace aes {
 namespace dev {
@@ -435,9 +437,10 @@ namespace aes {
 namespace dev {
 
 // ---------------------------------------------------------------------------------------------
-// query quantiser: one CTA per query, float64 arithmetic as numpy's (IEEE division and
-// multiplication, round half to even), so the integer query is bit-identical to
-// quantify_vector (quantify_util.py:31-49) applied to the float64 upcast of the FP32 query.
+// query quantiser: one CTA per query.  The integer query is bit-identical to quantify_vector
+// (quantify_util.py:31-49) applied to the float64 upcast of the FP32 query: numpy's binary64
+// division and multiplication (round to nearest even) and round-half-to-even are reproduced in
+// integer arithmetic (aes_qexact.hpp), so no FP64 runs on the GPU.
 // quant: 0 symmetric, 1/2 unsigned (per query); qq: 0 numpy, 1 quantize_vec truncation.
 // ---------------------------------------------------------------------------------------------
 __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_t ld32, int bits,
@@ -450,9 +453,7 @@ __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_
   if (qq == 1) {  // quantize_utils.hpp:8-18 (ap_fixed<32,B,AP_TRN_ZERO>, to_int, ap_int<B>)
     const int F = 32 - bits;
     for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) {
-      double v = (double)x[j] * ldexp(1.0, bits - 2 + F);
-      long long X = (long long)trunc(v);
-      int32_t X32 = (int32_t)(uint32_t)(unsigned long long)X;
+      const int32_t X32 = qx::trunc_scaled30(x[j]);  // x * 2^(B-2+F), truncated, 32-bit wrap
       int32_t n = X32 / (int32_t)(1u << F);
       int32_t mask = (1 << bits) - 1, half = 1 << (bits - 1);
       o[j] = (int8_t)(((n & mask) ^ half) - half);
@@ -480,7 +481,7 @@ __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_
     if (threadIdx.x == 0) red[0] = r;
   }
   __syncthreads();
-  const double mm = (double)red[0];  // max |x| (or max x) is exact in float64
+  const float mm = red[0];  // max |x| (or max x)
   if (quant != 0 && negs) {
     if (threadIdx.x == 0) atomicOr(status + blockIdx.x, ST_QUERY);
     for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) o[j] = 0;
@@ -490,9 +491,8 @@ __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_
   const int32_t lo = quant == 0 ? -M - 1 : 0;
   for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) {
     int32_t q = 0;
-    if (mm != 0.0) {
-      double y = (double)M * ((double)x[j] / mm);
-      q = (int32_t)rint(y);
+    if (mm != 0.0f) {
+      q = qx::round_scaled(x[j], mm, M);  // the float64 arithmetic of numpy, in integers
       q = q < lo ? lo : (q > M ? M : q);
     }
     o[j] = (int8_t)(uint8_t)(uint32_t)q;

@@ -66,7 +66,8 @@ int32_t orc_q_trunc(float v, int bits) {
   int F = 32 - bits;
   double x = (double)v * ldexp(1.0, bits - 2 + F); /* exact: power-of-two scaling */
   double t = trunc(x);
-  int64_t X = (int64_t)t;
+  /* beyond the int64 range x is a multiple of 2^32: its low 32 bits are zero */
+  int64_t X = fabs(t) >= 9.2e18 ? 0 : (int64_t)t;
   int32_t X32 = (int32_t)(uint32_t)(uint64_t)X;    /* 32-bit two's-complement wrap */
   int32_t n = X32 / (int32_t)(1u << F);           /* C division truncates toward zero */
   int32_t mask = (1 << bits) - 1;

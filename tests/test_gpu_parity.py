@@ -271,3 +271,27 @@ def test_large_k_and_ck(bits, quant, split, ck, k, nq):
         s = np.where(s == 0, np.float32(0), s)
         top = np.lexsort((-np.arange(rows, dtype=np.int64), -s.astype(np.float64)))[:k]
         assert np.array_equal(ei[i], top.astype(np.uint32)), f"exact query {i}"
+
+
+@pytest.mark.parametrize("bits,quant,qq", [(8, 0, 0), (6, 0, 0), (4, 0, 0), (8, 1, 0), (4, 2, 0),
+                                           (6, 0, 1)])
+def test_query_quantiser_on_rounding_ties(bits, quant, qq):
+    # query values placed on M * x / m = k + 1/2 (and one ulp either side): the device's integer
+    # quantiser must round them as numpy's float64 arithmetic does
+    rows, cols = 4000, 1024
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 77, bits, quant, 1, 256, 16,
+                  query_quant=qq)
+    M = ((1 << bits) - 1) // 2 if quant == 0 else (1 << bits) - 1
+    rng = np.random.default_rng(bits * 10 + quant)
+    for trial in range(3):
+        mx = np.float32(rng.uniform(0.5, 3.0))
+        k = rng.integers(0, M, cols)
+        q = (mx * (k + 0.5) / M).astype(np.float32)
+        nudge = rng.integers(-1, 2, cols).astype(np.int32)
+        q = (q.view(np.int32) + nudge).view(np.float32)
+        q = np.minimum(q, mx)
+        q[0] = mx
+        if quant == 0:
+            q = q * np.where(rng.random(cols) < 0.5, -1, 1).astype(np.float32)
+        got = eng.score_all(q)
+        assert np.array_equal(got, m.keys(q, qq=qq)), f"trial {trial}"
