@@ -368,9 +368,7 @@ int Engine::plan_config(const aes_params& p, Config* c) const {
   plan += p.k_max * 8ull;
   c->plan = plan;
 
-  const size_t stage = (size_t)((P + 3) / 4) * 32 * 16;
-  const size_t psmem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
-                       (S > 1 && S <= kThrSmemMax ? S * 4ull : 0ull);
+  const size_t psmem = plain_smem_bytes((int)bits, cols, S);
   if (psmem > (size_t)smem_optin)
     return fail(AES_ERR_UNSUPPORTED, "shared memory of the candidate pass exceeds the device limit");
   return AES_OK;
@@ -421,14 +419,10 @@ int Engine::apply_config(const Config& c) {
   AES_CK(cudaMemset(d_q32, 0, (size_t)maxB * ld32 * 4));
 
   // ---- launch geometry ---------------------------------------------------------------------
-  {
-    size_t stage = (size_t)((P + 3) / 4) * 32 * 16;
-    plain_smem = (size_t)cols * 64 + (size_t)kWarpsPlain * stage +
-                 (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
-  }
+  plain_smem = plain_smem_bytes((int)bits, cols, split);
   int occ = 0;
   AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), kThreadsPlain, plain_smem));
+      &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), plain_threads((int)bits), plain_smem));
   plain_grid = std::max(1, occ) * sm_count;
   batch_mode = p.batch_tile;
   batch_warps_n = batch_warps((int)bits, cols, split);
@@ -607,7 +601,8 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
   if (mode == MODE_SAMPLE) a.keys_out = d_sample_keys + (size_t)q * n_sample_rows;
   else if (mode == MODE_ALL) a.keys_out = d_allkeys;
   int grid = plain_grid;
-  if (mode == MODE_SAMPLE) grid = std::min<int>(grid, (int)((n_sample_tiles + kWarpsPlain - 1) / kWarpsPlain));
+  const int pw = plain_warps((int)bits);
+  if (mode == MODE_SAMPLE) grid = std::min<int>(grid, (int)((n_sample_tiles + pw - 1) / pw));
   grid = std::max(grid, 1);
   const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
   if (prof) {
@@ -625,7 +620,7 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
     }
     AES_CK(cudaEventRecord(prof_ev[prof_used], s));
   }
-  pick_plain((int)bits, sgn, mode)<<<grid, kThreadsPlain, plain_smem, s>>>(a);
+  pick_plain((int)bits, sgn, mode)<<<grid, plain_threads((int)bits), plain_smem, s>>>(a);
   AES_CK(cudaGetLastError());
   if (prof) {
     AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
@@ -1341,9 +1336,10 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
     a.n_sample_tiles = e.n_sample_tiles;
     int grid = e.plain_grid;
     if (mode == MODE_SAMPLE)
-      grid = std::min<int>(grid, (int)((e.n_sample_tiles + kWarpsPlain - 1) / kWarpsPlain));
+      grid = std::min<int>(grid, (int)((e.n_sample_tiles + plain_warps((int)e.bits) - 1) /
+                                       plain_warps((int)e.bits)));
     grid = std::max(grid, 1);
-    aes::pick_plain((int)e.bits, e.sgn, mode)<<<grid, kThreadsPlain, e.plain_smem, s>>>(a);
+    aes::pick_plain((int)e.bits, e.sgn, mode)<<<grid, plain_threads((int)e.bits), e.plain_smem, s>>>(a);
     AES_CK(cudaGetLastError());
     return AES_OK;
   };

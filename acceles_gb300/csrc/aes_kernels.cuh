@@ -24,8 +24,10 @@
 namespace aes {
 namespace dev {
 
-constexpr int kWarpsPlain = 32;      // warps per CTA of the plain candidate pass
-constexpr int kThreadsPlain = kWarpsPlain * 32;
+// warps per CTA of the plain candidate pass: as many as the query table, each warp's prefix
+// staging and next-tile buffer, and the partition thresholds leave room for in 227 KB
+__host__ __device__ constexpr int plain_warps(int B) { return B == 8 ? 28 : (B == 6 ? 26 : 24); }
+__host__ __device__ constexpr int plain_threads(int B) { return plain_warps(B) * 32; }
 
 enum Mode : int { MODE_FILTER = 0, MODE_SAMPLE = 1, MODE_ALL = 2 };
 
@@ -86,7 +88,7 @@ struct PlainArgs {
   uint32_t sample_stride, n_sample_tiles;
 };
 
-constexpr uint32_t kThrSmemMax = 4096;  // thresholds of up to this many partitions in smem
+constexpr uint32_t kThrSmemMax = 1024;  // thresholds of up to this many partitions in smem
 
 __device__ __forceinline__ uint32_t part_of(uint32_t row, uint32_t split, uint32_t slice) {
   if (split <= 1) return 0;
@@ -350,32 +352,47 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
 }
 
 // One warp streams tiles [tb, te) and owns every row whose first entry lies in them; the row
-// still open at te is finished by reading on until the next row flag.  Tiles are prefetched
-// three deep in registers.
+// still open at te is finished by reading on until the next row flag.  The next tile is copied
+// into the warp's shared buffer with cp.async while the current one is scored; each lane copies,
+// and later reads back, only its own 64 bytes, so no synchronisation between lanes is needed.
+// Tiles up to te (the first closing tile) are fetched one ahead; tiles past te only when the open
+// row runs on through the closing tile.
 template <int B, bool SGN, int MODE>
 __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
-                           const Emitter<MODE>& emit, const char* qtb, uint4* E4) {
+                           const Emitter<MODE>& emit, const char* qtb, uint4* E4, uint4* stg) {
   const uint32_t lane = threadIdx.x & 31u;
   if (tb >= te) return;
   RangeState st{tb == 0, 0u, 0u};  // row 0 starts at entry 0 without a flag
-  uint32_t wa[16], wb[16];
-  uint32_t ra = 0, rb = 0;
-  auto fetch = [&](uint32_t t, uint32_t (&w)[16], uint32_t& r) {
+  uint32_t w[16];
+  uint32_t rn = 0;
+  auto fetch = [&](uint32_t t) {
     if (t < a.n_tiles) {
-      load_tile(a.tiles, t, lane, w);
-      r = __ldg(a.tile_rowbase + t);
+      const uint4* src = a.tiles + (size_t)t * 128 + lane;
+#pragma unroll
+      for (int s = 0; s < 4; s++) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(stg + s * 32 + lane);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src + s * 32)
+                     : "memory");
+      }
+      rn = __ldg(a.tile_rowbase + t);
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
-  // tiles up to te (the first closing tile) are prefetched one ahead; tiles past te are read
-  // only when the open row runs on through the closing tile
-  fetch(tb, wa, ra);
-  for (uint32_t t = tb;; t += 2) {
-    if (t + 1 <= te) fetch(t + 1, wb, rb);
-    if (tile_step<B, SGN, MODE>(a, t, te, wa, ra, st, emit, qtb, E4)) return;
-    if (t + 1 > te) fetch(t + 1, wb, rb);
-    if (t + 2 <= te) fetch(t + 2, wa, ra);
-    if (tile_step<B, SGN, MODE>(a, t + 1, te, wb, rb, st, emit, qtb, E4)) return;
-    if (t + 2 > te) fetch(t + 2, wa, ra);
+  fetch(tb);
+  for (uint32_t t = tb;; t++) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      const uint4 v = stg[s * 32 + lane];
+      w[4 * s + 0] = v.x;
+      w[4 * s + 1] = v.y;
+      w[4 * s + 2] = v.z;
+      w[4 * s + 3] = v.w;
+    }
+    const uint32_t r = rn;
+    if (t + 1 <= te) fetch(t + 1);
+    if (tile_step<B, SGN, MODE>(a, t, te, w, r, st, emit, qtb, E4)) return;
+    if (t + 1 > te) fetch(t + 1);
   }
 }
 
@@ -383,9 +400,19 @@ template <int B>
 __host__ __device__ constexpr size_t plain_stage_bytes() {
   return (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;  // per warp
 }
+constexpr size_t kPlainTileBuf = 2048;  // per warp: the next 32-packet tile
+
+// dynamic shared memory of the plain pass: lane-replicated 16-bit query table, per-warp prefix
+// staging and next-tile buffer, thresholds of up to kThrSmemMax partitions
+__host__ inline size_t plain_smem_bytes(int B, uint32_t cols, uint32_t split) {
+  const size_t stage = (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;
+  return (size_t)cols * 64 + (size_t)plain_warps(B) * (stage + kPlainTileBuf) +
+         (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
+}
 
 template <int B, bool SGN, int MODE>
-__global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
+__global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a) {
+  constexpr int W = plain_warps(B);
   extern __shared__ __align__(16) unsigned char smem[];
   // the warp index through a shuffle from lane 0, so the range bounds and every branch on them
   // are known to be warp-uniform
@@ -394,8 +421,10 @@ __global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
   int16_t* qt = reinterpret_cast<int16_t*>(smem);
   uint4* E4all = reinterpret_cast<uint4*>(smem + (size_t)a.cols * 64);
   uint4* E4 = E4all + (size_t)warp * (plain_stage_bytes<B>() / 16);
+  uint4* stg = reinterpret_cast<uint4*>(smem + (size_t)a.cols * 64 + W * plain_stage_bytes<B>()) +
+               (size_t)warp * (kPlainTileBuf / 16);
   uint32_t* thr_s = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * 64 +
-                                                kWarpsPlain * plain_stage_bytes<B>());
+                                                W * (plain_stage_bytes<B>() + kPlainTileBuf));
   // replicate the query once per lane (lanes 2m and 2m+1 share bank m + 16 * (col & 1), so a
   // gather costs at most two wavefronts); the bytes are
   // staged through the (not yet used) prefix area so the fill needs one global round trip
@@ -414,19 +443,19 @@ __global__ void __launch_bounds__(kThreadsPlain, 1) k_cand_plain(PlainArgs a) {
     thr0 = a.thr[0];
   }
   __syncthreads();
-  const uint32_t gw = blockIdx.x * kWarpsPlain + warp;
-  const uint32_t nw = gridDim.x * kWarpsPlain;
+  const uint32_t gw = blockIdx.x * W + warp;
+  const uint32_t nw = gridDim.x * W;
   if constexpr (MODE == MODE_SAMPLE) {
     for (uint32_t s = gw; s < a.n_sample_tiles; s += nw) {
       const uint32_t t = s * a.sample_stride;
       Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s)};
-      cand_range<B, SGN, MODE>(a, t, t + 1, em, qtb, E4);
+      cand_range<B, SGN, MODE>(a, t, t + 1, em, qtb, E4, stg);
     }
   } else {
     const uint64_t n = a.n_tiles;
     const uint32_t tb = (uint32_t)((n * gw) / nw), te = (uint32_t)((n * (gw + 1)) / nw);
     Emitter<MODE> em{a, thr_s, thr0, 0u};
-    cand_range<B, SGN, MODE>(a, tb, te, em, qtb, E4);
+    cand_range<B, SGN, MODE>(a, tb, te, em, qtb, E4, stg);
   }
 }
 

@@ -17,9 +17,8 @@
 #pragma once
 
 #include <stdint.h>
-#ifndef __CUDACC__
+
 #include <cstring>
-#endif
 
 #ifdef __CUDACC__
 #define AES_QX_FN __host__ __device__ __forceinline__
