@@ -26,7 +26,7 @@ namespace dev {
 
 // warps per CTA of the plain candidate pass: as many as the query table, each warp's prefix
 // staging and next-tile buffer, and the partition thresholds leave room for in 227 KB
-__host__ __device__ constexpr int plain_warps(int B) { return B == 8 ? 28 : (B == 6 ? 26 : 24); }
+__host__ __device__ constexpr int plain_warps(int B) { return B == 8 ? 32 : (B == 6 ? 26 : 24); }
 __host__ __device__ constexpr int plain_threads(int B) { return plain_warps(B) * 32; }
 
 enum Mode : int { MODE_FILTER = 0, MODE_SAMPLE = 1, MODE_ALL = 2 };
@@ -213,7 +213,10 @@ struct PacketDecoder {
       if constexpr (n < 4) v4 &= (1u << (8 * n)) - 1u;
       const int32_t Sb = S;
       S = SGN ? __dp4a((int)v4, (int)q4, S) : (int32_t)__dp4a(v4, q4, (unsigned)S);
-      E4[G * 32] = make_uint4((uint32_t)Sb, v4, q4, 0u);
+      uint32_t* Ew = reinterpret_cast<uint32_t*>(E4);  // this lane's column of the warp's area
+      Ew[(G * 3 + 0) * 32] = (uint32_t)Sb;
+      Ew[(G * 3 + 1) * 32] = v4;
+      Ew[(G * 3 + 2) * 32] = q4;
       group<G + 1>(w, qtb, lane2, E4, S);
     }
   }
@@ -233,10 +236,11 @@ struct PacketDecoder {
   // running sum of this lane's packet before entry j (0 for j == 0)
   __device__ __forceinline__ static uint32_t prefix(const uint32_t* Ew, uint32_t lane, int j) {
     if constexpr (kGroups) {
-      const uint4 g = reinterpret_cast<const uint4*>(Ew)[(j >> 2) * 32 + lane];
+      const uint32_t* gw = Ew + ((j >> 2) * 3) * 32 + lane;
+      const uint32_t gx = gw[0], gy = gw[32], gz = gw[64];
       const uint32_t m = (1u << (8 * (j & 3))) - 1u;  // bytes of the group before entry j
-      return SGN ? (uint32_t)__dp4a((int)(g.y & m), (int)g.z, (int)g.x)
-                 : __dp4a(g.y & m, g.z, g.x);
+      return SGN ? (uint32_t)__dp4a((int)(gy & m), (int)gz, (int)gx)
+                 : __dp4a(gy & m, gz, gx);
     } else {
       if (j == 0) return 0u;
       const int i = j - 1;
@@ -290,7 +294,10 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
   }
   const uint32_t* Ew = reinterpret_cast<const uint32_t*>(E4);  // warp's staging area
   const Flags F = D::flags(w);
-  const int32_t total = D::run(w, qtb, lane << 1, E4 + lane);
+  // B = 8 stages three 32-bit words per group, B = 4, 6 one 16-byte slot per four entries
+  uint4* E4l = D::kGroups ? reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(E4) + lane)
+                          : E4 + lane;
+  const int32_t total = D::run(w, qtb, lane << 1, E4l);
   const uint32_t incl = warp_incl_sum((uint32_t)total, lane);
   const uint32_t LB = st.carryG + incl - (uint32_t)total;  // running sum before this packet
   const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
@@ -396,17 +403,22 @@ __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
   }
 }
 
+// per warp: B = 8 stages (sum before the group, values, query bytes) per group of four entries,
+// B = 4, 6 the running sum of every entry
+__host__ __device__ constexpr size_t plain_stage_bytes_of(int B) {
+  return B == 8 ? (size_t)((packet_elems(B) + 3) / 4) * 3 * 32 * 4
+                : (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;
+}
 template <int B>
 __host__ __device__ constexpr size_t plain_stage_bytes() {
-  return (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;  // per warp
+  return plain_stage_bytes_of(B);
 }
 constexpr size_t kPlainTileBuf = 2048;  // per warp: the next 32-packet tile
 
 // dynamic shared memory of the plain pass: lane-replicated 16-bit query table, per-warp prefix
 // staging and next-tile buffer, thresholds of up to kThrSmemMax partitions
 __host__ inline size_t plain_smem_bytes(int B, uint32_t cols, uint32_t split) {
-  const size_t stage = (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;
-  return (size_t)cols * 64 + (size_t)plain_warps(B) * (stage + kPlainTileBuf) +
+  return (size_t)cols * 64 + (size_t)plain_warps(B) * (plain_stage_bytes_of(B) + kPlainTileBuf) +
          (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
 }
 
