@@ -158,18 +158,13 @@ __device__ __forceinline__ uint32_t window32(const uint32_t (&w)[16]) {
   else return __funnelshift_r(w[k], w[k + 1], s);
 }
 
-// Per-lane decode of one packet.  Element j: 10-bit column at bit P + 10j, B-bit value at bit
-// 11P + Bj (fpga_utils.hpp:349-384).  run() returns the packet's sum of val_i * q[col_i]
-// (int32, wrapping) and stages what prefix() needs to give the running sum before any entry:
-//  - B = 8: four consecutive values are one 32-bit window, so each group of four entries is
-//    one dp4a of the packed values with the four query bytes; a group stages (sum before the
-//    group, values, query bytes) and prefix() finishes with a masked dp4a;
-//  - B = 4, 6: the running sum S_j of every entry, four per 16-byte slot.
+// Per-lane decode of one B = 4 or 6 packet.  Element j: 10-bit column at bit P + 10j, B-bit
+// value at bit 11P + Bj (fpga_utils.hpp:349-384).  run() returns the packet's sum of
+// val_i * q[col_i] (int32, wrapping) and stages the running sum S_j of every entry, four per
+// 16-byte slot, from which prefix() gives the running sum before any entry.
 template <int B, bool SGN>
 struct PacketDecoder {
   static constexpr int P = packet_elems(B);
-  static constexpr int NG = (P + 3) / 4;
-  static constexpr bool kGroups = (B == 8);
   using Flags = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
 
   // q[col_J] from the lane-replicated table qt[col][32] (int16): the column window starts 6
@@ -197,55 +192,19 @@ struct PacketDecoder {
     }
   }
 
-  template <int G>
-  __device__ __forceinline__ static void group(const uint32_t (&w)[16], const char* qtb,
-                                               uint32_t lane2, uint4* E4, int32_t& S) {
-    if constexpr (G < NG) {
-      constexpr int J = 4 * G;
-      constexpr int n = (P - J) < 4 ? (P - J) : 4;  // entries in this group
-      const int32_t q0 = qval<J>(w, qtb, lane2);
-      const int32_t q1 = n > 1 ? qval<(n > 1 ? J + 1 : J)>(w, qtb, lane2) : 0;
-      const int32_t q2 = n > 2 ? qval<(n > 2 ? J + 2 : J)>(w, qtb, lane2) : 0;
-      const int32_t q3 = n > 3 ? qval<(n > 3 ? J + 3 : J)>(w, qtb, lane2) : 0;
-      const uint32_t q4 = __byte_perm(__byte_perm((uint32_t)q0, (uint32_t)q1, 0x0040),
-                                      __byte_perm((uint32_t)q2, (uint32_t)q3, 0x0040), 0x5410);
-      uint32_t v4 = window32<11 * P + 32 * G>(w);
-      if constexpr (n < 4) v4 &= (1u << (8 * n)) - 1u;
-      const int32_t Sb = S;
-      S = SGN ? __dp4a((int)v4, (int)q4, S) : (int32_t)__dp4a(v4, q4, (unsigned)S);
-      uint32_t* Ew = reinterpret_cast<uint32_t*>(E4);  // this lane's column of the warp's area
-      Ew[(G * 3 + 0) * 32] = (uint32_t)Sb;
-      Ew[(G * 3 + 1) * 32] = v4;
-      Ew[(G * 3 + 2) * 32] = q4;
-      group<G + 1>(w, qtb, lane2, E4, S);
-    }
-  }
-
   __device__ __forceinline__ static int32_t run(const uint32_t (&w)[16], const char* qtb,
                                                 uint32_t lane2, uint4* E4) {
     int32_t S = 0;
-    if constexpr (kGroups) {
-      group<0>(w, qtb, lane2, E4, S);
-    } else {
-      int32_t s4[4] = {0, 0, 0, 0};
-      step<0>(w, qtb, lane2, E4, S, s4);
-    }
+    int32_t s4[4] = {0, 0, 0, 0};
+    step<0>(w, qtb, lane2, E4, S, s4);
     return S;
   }
 
   // running sum of this lane's packet before entry j (0 for j == 0)
   __device__ __forceinline__ static uint32_t prefix(const uint32_t* Ew, uint32_t lane, int j) {
-    if constexpr (kGroups) {
-      const uint32_t* gw = Ew + ((j >> 2) * 3) * 32 + lane;
-      const uint32_t gx = gw[0], gy = gw[32], gz = gw[64];
-      const uint32_t m = (1u << (8 * (j & 3))) - 1u;  // bytes of the group before entry j
-      return SGN ? (uint32_t)__dp4a((int)(gy & m), (int)gz, (int)gx)
-                 : __dp4a(gy & m, gz, gx);
-    } else {
-      if (j == 0) return 0u;
-      const int i = j - 1;
-      return Ew[(((i >> 2) * 32 + lane) << 2) | (i & 3)];
-    }
+    if (j == 0) return 0u;
+    const int i = j - 1;
+    return Ew[(((i >> 2) * 32 + lane) << 2) | (i & 3)];
   }
 
   __device__ __forceinline__ static Flags flags(const uint32_t (&w)[16]) {
@@ -253,6 +212,123 @@ struct PacketDecoder {
       return w[0] & ((P == 32) ? 0xFFFFFFFFu : ((1u << P) - 1u));
     } else {
       return (uint64_t)w[0] | ((uint64_t)(w[1] & ((1u << (P - 32)) - 1u)) << 32);
+    }
+  }
+};
+
+// Per-lane decode of one B = 8 packet (26 entries, same field layout).  Four consecutive values
+// are one 32-bit window, so a group of four entries is one dp4a of the packed values with the
+// four query bytes.  A row that starts and ends inside the packet is scored while the groups
+// are decoded: the running sum at a flag is the sum before its group plus a dp4a of the bytes
+// before it.  Nothing is staged in shared memory; only the row closed by a lane's first flag
+// needs the running sums of the lanes before it, which the warp scan gives after the decode.
+struct Rows8 {
+  int32_t S;       // running sum of the packet so far
+  uint32_t first;  // running sum before the first flagged entry
+  uint32_t prev;   // running sum before the last flagged entry so far
+  uint32_t row;    // row closed by the next flag
+  bool seen;       // a flag was met
+};
+
+template <bool SGN>
+struct Packet8 {
+  static constexpr int P = packet_elems(8);
+  static constexpr int NG = (P + 3) / 4;
+
+  // q[col_J] from the lane-replicated 32-bit table qt[col][32]: lane l reads bank l whatever the
+  // columns, so a gather is one wavefront.  The column window starts 7 bits early so
+  // (col << 7), the row offset of col in the table, lands at bits 7..16.
+  template <int J>
+  __device__ __forceinline__ static uint32_t qval(const uint32_t (&w)[16], const char* qtb,
+                                                  uint32_t lane4) {
+    const uint32_t y = window32<P + 10 * J - 7>(w);
+    return *reinterpret_cast<const uint32_t*>(qtb + ((y & 0x1FF80u) | lane4));
+  }
+
+  __device__ __forceinline__ static int32_t dot4(uint32_t v4, uint32_t q4, int32_t c) {
+    return SGN ? __dp4a((int)v4, (int)q4, c) : (int32_t)__dp4a(v4, q4, (unsigned)c);
+  }
+
+  // q0..q3 of group G packed into one word, and its four values
+  template <int G>
+  __device__ __forceinline__ static void load_group(const uint32_t (&w)[16], const char* qtb,
+                                                    uint32_t lane4, uint32_t& q4, uint32_t& v4) {
+    constexpr int J = 4 * G;
+    constexpr int n = (P - J) < 4 ? (P - J) : 4;  // entries in this group
+    const uint32_t q0 = qval<J>(w, qtb, lane4);
+    const uint32_t q1 = n > 1 ? qval<(n > 1 ? J + 1 : J)>(w, qtb, lane4) : 0u;
+    const uint32_t q2 = n > 2 ? qval<(n > 2 ? J + 2 : J)>(w, qtb, lane4) : 0u;
+    const uint32_t q3 = n > 3 ? qval<(n > 3 ? J + 3 : J)>(w, qtb, lane4) : 0u;
+    q4 = __byte_perm(__byte_perm(q0, q1, 0x0040), __byte_perm(q2, q3, 0x0040), 0x5410);
+    v4 = window32<11 * P + 32 * G>(w);
+    if constexpr (n < 4) v4 &= (1u << (8 * n)) - 1u;
+  }
+
+  // decode groups G .. G + NGR - 1 (eight entries, or the last ten) and score the rows closed by
+  // their flags (on_row(row, score) when inner).  The running sum at flag j of the span is the
+  // sum before the span plus the dp4a of the bytes before j, masked out of the packed values.
+  template <int G, int NGR>
+  __device__ __forceinline__ static uint32_t span_prefix(int j, int32_t Sa, uint32_t qa,
+                                                         uint32_t va, uint32_t qb, uint32_t vb,
+                                                         uint32_t qc, uint32_t vc) {
+    const uint64_t m = ~(~0ull << (8 * (j & 7)));  // bytes before entry j (j < 8)
+    if constexpr (NGR == 2) {
+      return (uint32_t)dot4(vb & (uint32_t)(m >> 32), qb, dot4(va & (uint32_t)m, qa, Sa));
+    } else {
+      const bool lo = j < 8;
+      const uint32_t ma = lo ? (uint32_t)m : 0xFFFFFFFFu;
+      const uint32_t mb = lo ? (uint32_t)(m >> 32) : 0xFFFFFFFFu;
+      const uint32_t mc = lo ? 0u : ~(0xFFFFFFFFu << (8 * ((j - 8) & 3)));
+      const int32_t x = dot4(vb & mb, qb, dot4(va & ma, qa, Sa));
+      return (uint32_t)dot4(vc & mc, qc, x);
+    }
+  }
+
+  template <int G, class OnRow>
+  __device__ __forceinline__ static void span(const uint32_t (&w)[16], const char* qtb,
+                                              uint32_t lane4, uint32_t F, bool inner, Rows8& s,
+                                              const OnRow& on_row) {
+    if constexpr (G < NG) {
+      // spans of two groups; the last takes the short tail group as a third
+      constexpr int NGR = (G + 3 == NG) ? 3 : 2;
+      constexpr int NE = (P - 4 * G) < 4 * NGR ? (P - 4 * G) : 4 * NGR;  // entries in the span
+      static_assert(NGR == 3 || G + 2 < NG, "span layout");
+      static_assert(NE <= 10, "a span holds at most ten entries");
+      uint32_t qa, va, qb, vb, qc = 0u, vc = 0u;
+      load_group<G>(w, qtb, lane4, qa, va);
+      load_group<G + 1>(w, qtb, lane4, qb, vb);
+      if constexpr (NGR == 3) load_group<(NGR == 3 ? G + 2 : G)>(w, qtb, lane4, qc, vc);
+      const int32_t Sa = s.S;
+      s.S = dot4(vb, qb, dot4(va, qa, Sa));
+      if constexpr (NGR == 3) s.S = dot4(vc, qc, s.S);
+      const uint32_t fP = (F >> (4 * G)) & ((1u << NE) - 1u);
+      // the lowest flag without a branch around it; further flags in the span (rows shorter than
+      // the span) in a loop
+      const bool has = fP != 0;
+      {
+        const int j = __ffs(fP) - 1;
+        const uint32_t Pj = span_prefix<G, NGR>(j, Sa, qa, va, qb, vb, qc, vc);
+        if (has) {
+          if (s.seen) {
+            if (inner) on_row(s.row, (int32_t)(Pj - s.prev));
+          } else {
+            s.first = Pj;
+          }
+          s.seen = true;
+          s.prev = Pj;
+          s.row++;
+        }
+      }
+      uint32_t rest = fP & (fP - 1u);
+      while (rest) {
+        const int j = __ffs(rest) - 1;
+        rest &= rest - 1u;
+        const uint32_t Pj = span_prefix<G, NGR>(j, Sa, qa, va, qb, vb, qc, vc);
+        if (inner) on_row(s.row, (int32_t)(Pj - s.prev));
+        s.prev = Pj;
+        s.row++;
+      }
+      span<G + NGR>(w, qtb, lane4, F, inner, s, on_row);
     }
   }
 };
@@ -279,7 +355,7 @@ struct RangeState {
   uint32_t carryG;  // running sum before the current tile
 };
 
-// One tile of a warp's range.  Returns true once the range is complete.
+// One tile of a warp's range (B = 4, 6).  Returns true once the range is complete.
 template <int B, bool SGN, int MODE>
 __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32_t te,
                                           const uint32_t (&w)[16], uint32_t rowbase,
@@ -294,10 +370,7 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
   }
   const uint32_t* Ew = reinterpret_cast<const uint32_t*>(E4);  // warp's staging area
   const Flags F = D::flags(w);
-  // B = 8 stages three 32-bit words per group, B = 4, 6 one 16-byte slot per four entries
-  uint4* E4l = D::kGroups ? reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(E4) + lane)
-                          : E4 + lane;
-  const int32_t total = D::run(w, qtb, lane << 1, E4l);
+  const int32_t total = D::run(w, qtb, lane << 1, E4 + lane);
   const uint32_t incl = warp_incl_sum((uint32_t)total, lane);
   const uint32_t LB = st.carryG + incl - (uint32_t)total;  // running sum before this packet
   const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
@@ -358,13 +431,71 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
   return false;
 }
 
+// One tile of a warp's range (B = 8).  Returns true once the range is complete.  INTF: the
+// integer filter with one partition, a compare per row and the survivor append only on a hit.
+template <bool SGN, int MODE, bool INTF>
+__device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t, uint32_t te,
+                                           const uint32_t (&w)[16], uint32_t rowbase,
+                                           RangeState& st, const Emitter<MODE>& emit,
+                                           const char* qtb) {
+  const uint32_t lane = threadIdx.x & 31u;
+  if (t >= a.n_tiles) {  // the end of the matrix closes the last row
+    if (st.open_owned && lane == 0) emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG));
+    return true;
+  }
+  const uint32_t F = w[0] & ((1u << Packet8<SGN>::P) - 1u);
+  const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
+  const bool closing = t >= te;  // only the first flag from here on matters
+  uint32_t rbase = rowbase;      // row closed by this lane's first flag
+  if (!closing) {
+    const uint32_t nf = __popc(F);
+    rbase += warp_incl_sum(nf, lane) - nf;
+  }
+  const int32_t ts = emit.thr_score();
+  auto on_row = [&](uint32_t row, int32_t sc) {
+    if constexpr (INTF) {
+      if (sc >= ts) emit.append_int(row, sc);
+    } else {
+      emit(row, sc);
+    }
+  };
+  Rows8 s{0, 0u, 0u, rbase, false};
+  Packet8<SGN>::template span<0>(w, qtb, lane << 2, F, !closing, s, on_row);
+  const uint32_t total = (uint32_t)s.S;
+  const uint32_t incl = warp_incl_sum(total, lane);
+  const uint32_t LB = st.carryG + incl - total;  // running sum before this packet
+  const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  if (closing) {
+    if (has_mask == 0) {
+      st.carryG += tileSum;
+      return false;
+    }
+    if (lane == (uint32_t)(__ffs(has_mask) - 1) && st.open_owned)
+      emit(rowbase, (int32_t)(LB + s.first - st.startG));
+    return true;
+  }
+  // the row closed by a lane's first flag started at the last flag of the lanes before it, or
+  // before the tile
+  const uint32_t lastGb = LB + s.prev;
+  const uint32_t left = has_mask & ((1u << lane) - 1u);
+  const uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, left ? (31 - __clz(left)) : 0u);
+  const uint32_t prevG = left ? inhG : st.startG;
+  if (F && (left || st.open_owned)) on_row(rbase, (int32_t)(LB + s.first - prevG));
+  if (has_mask) {
+    st.startG = __shfl_sync(0xFFFFFFFFu, lastGb, 31 - __clz(has_mask));
+    st.open_owned = true;
+  }
+  st.carryG += tileSum;
+  return false;
+}
+
 // One warp streams tiles [tb, te) and owns every row whose first entry lies in them; the row
 // still open at te is finished by reading on until the next row flag.  The next tile is copied
 // into the warp's shared buffer with cp.async while the current one is scored; each lane copies,
 // and later reads back, only its own 64 bytes, so no synchronisation between lanes is needed.
 // Tiles up to te (the first closing tile) are fetched one ahead; tiles past te only when the open
 // row runs on through the closing tile.
-template <int B, bool SGN, int MODE>
+template <int B, bool SGN, int MODE, bool INTF>
 __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
                            const Emitter<MODE>& emit, const char* qtb, uint4* E4, uint4* stg) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -398,54 +529,63 @@ __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
     }
     const uint32_t r = rn;
     if (t + 1 <= te) fetch(t + 1);
-    if (tile_step<B, SGN, MODE>(a, t, te, w, r, st, emit, qtb, E4)) return;
+    if constexpr (B == 8) {
+      if (tile_step8<SGN, MODE, INTF>(a, t, te, w, r, st, emit, qtb)) return;
+    } else {
+      if (tile_step<B, SGN, MODE>(a, t, te, w, r, st, emit, qtb, E4)) return;
+    }
     if (t + 1 > te) fetch(t + 1);
   }
 }
 
-// per warp: B = 8 stages (sum before the group, values, query bytes) per group of four entries,
-// B = 4, 6 the running sum of every entry
+// per warp: B = 4, 6 stage the running sum of every entry (B = 8 stages nothing)
 __host__ __device__ constexpr size_t plain_stage_bytes_of(int B) {
-  return B == 8 ? (size_t)((packet_elems(B) + 3) / 4) * 3 * 32 * 4
-                : (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;
+  return B == 8 ? 0 : (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;
 }
-template <int B>
-__host__ __device__ constexpr size_t plain_stage_bytes() {
-  return plain_stage_bytes_of(B);
-}
+// query table bytes per column: 32 lane copies, 32-bit for B = 8 (one wavefront per gather),
+// 16-bit for B = 4, 6 (lanes 2m and 2m+1 share bank m + 16 * (col & 1): at most two)
+__host__ __device__ constexpr size_t plain_table_bytes_per_col(int B) { return B == 8 ? 128 : 64; }
 constexpr size_t kPlainTileBuf = 2048;  // per warp: the next 32-packet tile
 
-// dynamic shared memory of the plain pass: lane-replicated 16-bit query table, per-warp prefix
+// dynamic shared memory of the plain pass: lane-replicated query table, per-warp prefix
 // staging and next-tile buffer, thresholds of up to kThrSmemMax partitions
 __host__ inline size_t plain_smem_bytes(int B, uint32_t cols, uint32_t split) {
-  return (size_t)cols * 64 + (size_t)plain_warps(B) * (plain_stage_bytes_of(B) + kPlainTileBuf) +
+  return (size_t)cols * plain_table_bytes_per_col(B) +
+         (size_t)plain_warps(B) * (plain_stage_bytes_of(B) + kPlainTileBuf) +
          (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
 }
 
 template <int B, bool SGN, int MODE>
 __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a) {
   constexpr int W = plain_warps(B);
+  constexpr size_t TB = plain_table_bytes_per_col(B), SB = plain_stage_bytes_of(B);
   extern __shared__ __align__(16) unsigned char smem[];
   // the warp index through a shuffle from lane 0, so the range bounds and every branch on them
   // are known to be warp-uniform
   const uint32_t warp = __shfl_sync(0xFFFFFFFFu, threadIdx.x >> 5, 0);
-  const char* qtb = reinterpret_cast<const char*>(smem);            // int16 qt[cols][32]
-  int16_t* qt = reinterpret_cast<int16_t*>(smem);
-  uint4* E4all = reinterpret_cast<uint4*>(smem + (size_t)a.cols * 64);
-  uint4* E4 = E4all + (size_t)warp * (plain_stage_bytes<B>() / 16);
-  uint4* stg = reinterpret_cast<uint4*>(smem + (size_t)a.cols * 64 + W * plain_stage_bytes<B>()) +
-               (size_t)warp * (kPlainTileBuf / 16);
-  uint32_t* thr_s = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * 64 +
-                                                W * (plain_stage_bytes<B>() + kPlainTileBuf));
-  // replicate the query once per lane (lanes 2m and 2m+1 share bank m + 16 * (col & 1), so a
-  // gather costs at most two wavefronts); the bytes are
-  // staged through the (not yet used) prefix area so the fill needs one global round trip
-  int8_t* qstage = reinterpret_cast<int8_t*>(E4all);
+  const char* qtb = reinterpret_cast<const char*>(smem);  // qt[cols][32 lanes]
+  unsigned char* after = smem + (size_t)a.cols * TB;
+  uint4* E4 = reinterpret_cast<uint4*>(after) + (size_t)warp * (SB / 16);
+  uint4* stg = reinterpret_cast<uint4*>(after + W * SB) + (size_t)warp * (kPlainTileBuf / 16);
+  uint32_t* thr_s = reinterpret_cast<uint32_t*>(after + W * (SB + kPlainTileBuf));
+  // replicate the query once per lane; the bytes are staged through the (not yet used) area
+  // after the table so the fill needs one global round trip
+  int8_t* qstage = reinterpret_cast<int8_t*>(after);
   for (uint32_t i = threadIdx.x; i < a.cols; i += blockDim.x) qstage[i] = a.q8[i];
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < a.cols * 32u; i += blockDim.x) {
-    const uint32_t c = i >> 5;
-    qt[i] = SGN ? (int16_t)qstage[c] : (int16_t)(uint8_t)qstage[c];
+  if constexpr (B == 8) {
+    uint4* qt = reinterpret_cast<uint4*>(smem);  // four lane copies per store
+    for (uint32_t i = threadIdx.x; i < a.cols * 8u; i += blockDim.x) {
+      const int8_t q = qstage[i >> 3];
+      const uint32_t v = SGN ? (uint32_t)(int32_t)q : (uint32_t)(uint8_t)q;
+      qt[i] = make_uint4(v, v, v, v);
+    }
+  } else {
+    int16_t* qt = reinterpret_cast<int16_t*>(smem);
+    for (uint32_t i = threadIdx.x; i < a.cols * 32u; i += blockDim.x) {
+      const uint32_t c = i >> 5;
+      qt[i] = SGN ? (int16_t)qstage[c] : (int16_t)(uint8_t)qstage[c];
+    }
   }
   __syncthreads();
   uint32_t thr0 = 0;
@@ -461,13 +601,19 @@ __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a)
     for (uint32_t s = gw; s < a.n_sample_tiles; s += nw) {
       const uint32_t t = s * a.sample_stride;
       Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s)};
-      cand_range<B, SGN, MODE>(a, t, t + 1, em, qtb, E4, stg);
+      cand_range<B, SGN, MODE, false>(a, t, t + 1, em, qtb, E4, stg);
     }
   } else {
     const uint64_t n = a.n_tiles;
     const uint32_t tb = (uint32_t)((n * gw) / nw), te = (uint32_t)((n * (gw + 1)) / nw);
     Emitter<MODE> em{a, thr_s, thr0, 0u};
-    cand_range<B, SGN, MODE>(a, tb, te, em, qtb, E4, stg);
+    if constexpr (B == 8 && MODE == MODE_FILTER) {
+      if (em.int_filter()) {
+        cand_range<B, SGN, MODE, true>(a, tb, te, em, qtb, E4, stg);
+        return;
+      }
+    }
+    cand_range<B, SGN, MODE, false>(a, tb, te, em, qtb, E4, stg);
   }
 }
 
