@@ -255,11 +255,12 @@ struct Packet8 {
                                                     uint32_t lane4, uint32_t& q4, uint32_t& v4) {
     constexpr int J = 4 * G;
     constexpr int n = (P - J) < 4 ? (P - J) : 4;  // entries in this group
-    const uint32_t q0 = qval<J>(w, qtb, lane4);
-    const uint32_t q1 = n > 1 ? qval<(n > 1 ? J + 1 : J)>(w, qtb, lane4) : 0u;
-    const uint32_t q2 = n > 2 ? qval<(n > 2 ? J + 2 : J)>(w, qtb, lane4) : 0u;
-    const uint32_t q3 = n > 3 ? qval<(n > 3 ? J + 3 : J)>(w, qtb, lane4) : 0u;
-    q4 = __byte_perm(__byte_perm(q0, q1, 0x0040), __byte_perm(q2, q3, 0x0040), 0x5410);
+    // table entries are zero-extended bytes, so multiply-adds place them (FMA pipe, leaving
+    // the integer ALU pipe to the field extraction)
+    q4 = qval<J>(w, qtb, lane4);
+    if constexpr (n > 1) q4 += qval<(n > 1 ? J + 1 : J)>(w, qtb, lane4) * 0x100u;
+    if constexpr (n > 2) q4 += qval<(n > 2 ? J + 2 : J)>(w, qtb, lane4) * 0x10000u;
+    if constexpr (n > 3) q4 += qval<(n > 3 ? J + 3 : J)>(w, qtb, lane4) * 0x1000000u;
     v4 = window32<11 * P + 32 * G>(w);
     if constexpr (n < 4) v4 &= (1u << (8 * n)) - 1u;
   }
@@ -284,16 +285,34 @@ struct Packet8 {
     }
   }
 
-  template <int G, class OnRow>
+  // flag bits of entries [4G, 4G + 4 * NGR) of the packet, for the span starting at group G
+  template <int G>
+  __host__ __device__ static constexpr int span_groups() { return (G + 3 == NG) ? 3 : 2; }
+  template <int G>
+  __host__ __device__ static constexpr uint32_t span_bits() {
+    return ((P - 4 * G) < 4 * span_groups<G>() ? ((1u << (P - 4 * G)) - 1u)
+                                               : ((1u << (4 * span_groups<G>())) - 1u))
+           << (4 * G);
+  }
+  // true when some span of this packet holds two or more flags (a row shorter than a span)
+  __device__ __forceinline__ static bool two_in_a_span(uint32_t F) {
+    constexpr uint32_t m0 = span_bits<0>(), m1 = span_bits<2>(), m2 = span_bits<4>();
+    static_assert((m0 | m1 | m2) == (1u << P) - 1u && NG == 7, "span layout");
+    const uint32_t a = F & m0, b = F & m1, c = F & m2;
+    return ((a & (a - 1u)) | (b & (b - 1u)) | (c & (c - 1u))) != 0u;
+  }
+
+  // Decode the span starting at group G and score the rows closed by its flags: each closed row
+  // goes to on_row(valid, row, score) (INNER: not on the closing tile).  The lowest flag of the
+  // span is handled without a branch; further flags (MULTI: some lane of the warp has them) in
+  // a loop.
+  template <int G, bool INNER, class OnRow>
   __device__ __forceinline__ static void span(const uint32_t (&w)[16], const char* qtb,
-                                              uint32_t lane4, uint32_t F, bool inner, Rows8& s,
+                                              uint32_t lane4, uint32_t F, bool multi, Rows8& s,
                                               const OnRow& on_row) {
     if constexpr (G < NG) {
-      // spans of two groups; the last takes the short tail group as a third
-      constexpr int NGR = (G + 3 == NG) ? 3 : 2;
-      constexpr int NE = (P - 4 * G) < 4 * NGR ? (P - 4 * G) : 4 * NGR;  // entries in the span
+      constexpr int NGR = span_groups<G>();
       static_assert(NGR == 3 || G + 2 < NG, "span layout");
-      static_assert(NE <= 10, "a span holds at most ten entries");
       uint32_t qa, va, qb, vb, qc = 0u, vc = 0u;
       load_group<G>(w, qtb, lane4, qa, va);
       load_group<G + 1>(w, qtb, lane4, qb, vb);
@@ -301,34 +320,26 @@ struct Packet8 {
       const int32_t Sa = s.S;
       s.S = dot4(vb, qb, dot4(va, qa, Sa));
       if constexpr (NGR == 3) s.S = dot4(vc, qc, s.S);
-      const uint32_t fP = (F >> (4 * G)) & ((1u << NE) - 1u);
-      // the lowest flag without a branch around it; further flags in the span (rows shorter than
-      // the span) in a loop
+      const uint32_t fP = (F & span_bits<G>()) >> (4 * G);
       const bool has = fP != 0;
-      {
-        const int j = __ffs(fP) - 1;
-        const uint32_t Pj = span_prefix<G, NGR>(j, Sa, qa, va, qb, vb, qc, vc);
-        if (has) {
-          if (s.seen) {
-            if (inner) on_row(s.row, (int32_t)(Pj - s.prev));
-          } else {
-            s.first = Pj;
-          }
-          s.seen = true;
-          s.prev = Pj;
+      const uint32_t Pj = span_prefix<G, NGR>(__ffs(fP) - 1, Sa, qa, va, qb, vb, qc, vc);
+      if constexpr (INNER) on_row(has && s.seen, s.row, (int32_t)(Pj - s.prev));
+      s.first = (has && !s.seen) ? Pj : s.first;
+      s.prev = has ? Pj : s.prev;
+      s.row += has ? 1u : 0u;
+      s.seen = s.seen || has;
+      if (multi) {
+        uint32_t rest = fP & (fP - 1u);
+        while (rest) {
+          const int j = __ffs(rest) - 1;
+          rest &= rest - 1u;
+          const uint32_t Pk = span_prefix<G, NGR>(j, Sa, qa, va, qb, vb, qc, vc);
+          if constexpr (INNER) on_row(true, s.row, (int32_t)(Pk - s.prev));
+          s.prev = Pk;
           s.row++;
         }
       }
-      uint32_t rest = fP & (fP - 1u);
-      while (rest) {
-        const int j = __ffs(rest) - 1;
-        rest &= rest - 1u;
-        const uint32_t Pj = span_prefix<G, NGR>(j, Sa, qa, va, qb, vb, qc, vc);
-        if (inner) on_row(s.row, (int32_t)(Pj - s.prev));
-        s.prev = Pj;
-        s.row++;
-      }
-      span<G + NGR>(w, qtb, lane4, F, inner, s, on_row);
+      span<G + NGR, INNER>(w, qtb, lane4, F, multi, s, on_row);
     }
   }
 };
@@ -340,11 +351,16 @@ __device__ __forceinline__ int fls_flags(uint64_t f) { return 63 - __clzll((long
 __device__ __forceinline__ uint32_t popc_flags(uint32_t f) { return __popc(f); }
 __device__ __forceinline__ uint32_t popc_flags(uint64_t f) { return __popcll(f); }
 
+// inclusive warp sum; shfl.up's own predicate (source lane in range) guards each add
 __device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, uint32_t lane) {
+  (void)lane;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    uint32_t u = __shfl_up_sync(0xFFFFFFFFu, v, d);
-    if (lane >= (uint32_t)d) v += u;
+    asm("{\n\t.reg .b32 t;\n\t.reg .pred p;\n\t"
+        "shfl.sync.up.b32 t|p, %0, %1, 0, 0xffffffff;\n\t"
+        "@p add.u32 %0, %0, t;\n\t}"
+        : "+r"(v)
+        : "r"(d));
   }
   return v;
 }
@@ -433,39 +449,43 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
 
 // One tile of a warp's range (B = 8).  Returns true once the range is complete.  INTF: the
 // integer filter with one partition, a compare per row and the survivor append only on a hit.
-template <bool SGN, int MODE, bool INTF>
-__device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t, uint32_t te,
+// CLOSING: a tile at or past the range's end, where only the first flag matters.
+template <bool SGN, int MODE, bool INTF, bool CLOSING>
+__device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
                                            const uint32_t (&w)[16], uint32_t rowbase,
                                            RangeState& st, const Emitter<MODE>& emit,
                                            const char* qtb) {
+  using D = Packet8<SGN>;
   const uint32_t lane = threadIdx.x & 31u;
-  if (t >= a.n_tiles) {  // the end of the matrix closes the last row
-    if (st.open_owned && lane == 0) emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG));
-    return true;
+  if constexpr (CLOSING) {
+    if (t >= a.n_tiles) {  // the end of the matrix closes the last row
+      if (st.open_owned && lane == 0) emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG));
+      return true;
+    }
   }
-  const uint32_t F = w[0] & ((1u << Packet8<SGN>::P) - 1u);
+  const uint32_t F = w[0] & ((1u << D::P) - 1u);
   const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
-  const bool closing = t >= te;  // only the first flag from here on matters
-  uint32_t rbase = rowbase;      // row closed by this lane's first flag
-  if (!closing) {
+  uint32_t rbase = rowbase;  // row closed by this lane's first flag
+  if constexpr (!CLOSING) {
     const uint32_t nf = __popc(F);
     rbase += warp_incl_sum(nf, lane) - nf;
   }
   const int32_t ts = emit.thr_score();
-  auto on_row = [&](uint32_t row, int32_t sc) {
+  auto on_row = [&](bool valid, uint32_t row, int32_t sc) {
     if constexpr (INTF) {
-      if (sc >= ts) emit.append_int(row, sc);
+      if (valid && sc >= ts) emit.append_int(row, sc);
     } else {
-      emit(row, sc);
+      if (valid) emit(row, sc);
     }
   };
+  const bool multi = !CLOSING && __any_sync(0xFFFFFFFFu, D::two_in_a_span(F));
   Rows8 s{0, 0u, 0u, rbase, false};
-  Packet8<SGN>::template span<0>(w, qtb, lane << 2, F, !closing, s, on_row);
+  D::template span<0, !CLOSING>(w, qtb, lane << 2, F, multi, s, on_row);
   const uint32_t total = (uint32_t)s.S;
   const uint32_t incl = warp_incl_sum(total, lane);
   const uint32_t LB = st.carryG + incl - total;  // running sum before this packet
   const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
-  if (closing) {
+  if constexpr (CLOSING) {
     if (has_mask == 0) {
       st.carryG += tileSum;
       return false;
@@ -473,20 +493,21 @@ __device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t, uint3
     if (lane == (uint32_t)(__ffs(has_mask) - 1) && st.open_owned)
       emit(rowbase, (int32_t)(LB + s.first - st.startG));
     return true;
+  } else {
+    // the row closed by a lane's first flag started at the last flag of the lanes before it,
+    // or before the tile
+    const uint32_t lastGb = LB + s.prev;
+    const uint32_t left = has_mask & ((1u << lane) - 1u);
+    const uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, left ? (31 - __clz(left)) : 0u);
+    const uint32_t prevG = left ? inhG : st.startG;
+    on_row(F && (left || st.open_owned), rbase, (int32_t)(LB + s.first - prevG));
+    if (has_mask) {
+      st.startG = __shfl_sync(0xFFFFFFFFu, lastGb, 31 - __clz(has_mask));
+      st.open_owned = true;
+    }
+    st.carryG += tileSum;
+    return false;
   }
-  // the row closed by a lane's first flag started at the last flag of the lanes before it, or
-  // before the tile
-  const uint32_t lastGb = LB + s.prev;
-  const uint32_t left = has_mask & ((1u << lane) - 1u);
-  const uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, left ? (31 - __clz(left)) : 0u);
-  const uint32_t prevG = left ? inhG : st.startG;
-  if (F && (left || st.open_owned)) on_row(rbase, (int32_t)(LB + s.first - prevG));
-  if (has_mask) {
-    st.startG = __shfl_sync(0xFFFFFFFFu, lastGb, 31 - __clz(has_mask));
-    st.open_owned = true;
-  }
-  st.carryG += tileSum;
-  return false;
 }
 
 // One warp streams tiles [tb, te) and owns every row whose first entry lies in them; the row
@@ -530,7 +551,11 @@ __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
     const uint32_t r = rn;
     if (t + 1 <= te) fetch(t + 1);
     if constexpr (B == 8) {
-      if (tile_step8<SGN, MODE, INTF>(a, t, te, w, r, st, emit, qtb)) return;
+      if (t < te) {  // te <= n_tiles
+        tile_step8<SGN, MODE, INTF, false>(a, t, w, r, st, emit, qtb);
+      } else if (tile_step8<SGN, MODE, INTF, true>(a, t, w, r, st, emit, qtb)) {
+        return;
+      }
     } else {
       if (tile_step<B, SGN, MODE>(a, t, te, w, r, st, emit, qtb, E4)) return;
     }
@@ -576,8 +601,7 @@ __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a)
   if constexpr (B == 8) {
     uint4* qt = reinterpret_cast<uint4*>(smem);  // four lane copies per store
     for (uint32_t i = threadIdx.x; i < a.cols * 8u; i += blockDim.x) {
-      const int8_t q = qstage[i >> 3];
-      const uint32_t v = SGN ? (uint32_t)(int32_t)q : (uint32_t)(uint8_t)q;
+      const uint32_t v = (uint8_t)qstage[i >> 3];  // the byte dp4a reads (signed or not)
       qt[i] = make_uint4(v, v, v, v);
     }
   } else {
