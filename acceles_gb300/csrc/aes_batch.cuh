@@ -7,9 +7,10 @@
 //            per-warp shared records in element order;
 //   phase B (lane = 4 queries): walk the tile's elements four at a time.  For a group of four
 //            elements every lane gathers its four queries' bytes at the four columns (one 32-bit
-//            load each from qtab[col][128]), transposes the 4x4 bytes with PRMT and accumulates
-//            with dp4a (exact int8 x int8 -> int32).  Row flags are the same for every lane,
-//            so row boundaries never diverge.
+//            load each from the query table, 33 words per column: lane l's word at col * 33 + l,
+//            so a gather is conflict-free and its address one multiply-add), transposes the 4x4
+//            bytes with PRMT and accumulates with dp4a (exact int8 x int8 -> int32).  Row flags
+//            are the same for every lane, so row boundaries never diverge.
 #pragma once
 
 #include "aes_kernels.cuh"
@@ -18,6 +19,11 @@ namespace aes {
 namespace dev {
 
 constexpr int kBatchQ = 128;         // queries per tile (32 lanes x 4)
+constexpr uint32_t kQtabWords = 33;  // query table words per column: 32 lanes and a pad word
+// words of one block's query table, padded to whole 16-byte slots
+__host__ __device__ constexpr size_t batch_qtab_words(uint32_t cols) {
+  return ((size_t)cols * kQtabWords + 3) & ~(size_t)3;
+}
 constexpr int kWarpsBatchMax = 16;
 constexpr size_t kSmemMax = 227 * 1024;
 
@@ -25,7 +31,7 @@ struct BatchArgs {
   const uint4* tiles;
   const uint32_t* tile_rowbase;
   uint32_t n_tiles, n_rows, cols;
-  const uint32_t* qtab;         // [cols][32] words: bytes of queries 4l..4l+3 at (col, lane l)
+  const uint32_t* qtab;         // [cols][33] words: bytes of queries 4l..4l+3 at (col, lane l)
   uint32_t q0, nq;              // this launch scores queries q0 .. q0 + nq - 1 (nq <= 128)
   const float* rowscale;
   uint32_t split, slice;
@@ -38,7 +44,7 @@ struct BatchArgs {
   uint32_t sample_stride, n_sample_tiles;
 };
 
-// per-warp element records: column byte offsets (u32), values (u8) and row flags (u8) of the 32
+// per-warp element records: columns (u32), values (u8) and row flags (u8) of the 32
 // packets of a tile, plus one zero group of four so the walk can read one group ahead
 template <int B>
 __host__ __device__ constexpr uint32_t batch_rec_elems() {
@@ -57,13 +63,13 @@ __host__ __device__ inline bool batch_thr_in_smem(uint32_t split) { return split
 // warps per CTA that fit next to the query table (and thresholds) in shared memory
 __host__ inline int batch_warps(int B, uint32_t cols, uint32_t split) {
   const size_t per = batch_warp_bytes_rt(B);
-  const size_t fixed = (size_t)cols * kBatchQ + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0);
+  const size_t fixed = batch_qtab_words(cols) * 4 + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0);
   int w = (int)((kSmemMax - fixed) / per);
   return w > kWarpsBatchMax ? kWarpsBatchMax : w;
 }
 __host__ inline size_t batch_smem_bytes(int B, uint32_t cols, uint32_t split, int warps) {
   const size_t per = batch_warp_bytes_rt(B);
-  return (size_t)cols * kBatchQ + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0) +
+  return batch_qtab_words(cols) * 4 + (batch_thr_in_smem(split) ? (size_t)split * kBatchQ * 4 : 0) +
          (size_t)warps * per;
 }
 
@@ -169,7 +175,8 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
   constexpr uint32_t NR = batch_rec_elems<B>();
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lane4 = lane << 2;
-  uint32_t* offs = reinterpret_cast<uint32_t*>(wsm);            // [NR] col * 128
+  constexpr uint32_t RB = kQtabWords * 4;  // query table bytes per column
+  uint32_t* offs = reinterpret_cast<uint32_t*>(wsm);            // [NR] col
   uint8_t* vals = wsm + (size_t)NR * 4;                          // [NR]
   uint8_t* flg = wsm + (size_t)NR * 5;                           // [NR]
   if (tb >= te) return;
@@ -198,7 +205,7 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
       for (int j = 0; j < P; j++) {
         const uint32_t cpos = P + 10 * j, vpos = 11 * P + B * j;
         const uint32_t cw = __funnelshift_r(w[cpos >> 5], w[(cpos >> 5) + 1 < 16 ? (cpos >> 5) + 1 : 15], cpos & 31);
-        o[j] = (cw & 0x3FFu) << 7;
+        o[j] = cw & 0x3FFu;
         const uint32_t vw = __funnelshift_r(w[vpos >> 5], w[(vpos >> 5) + 1 < 16 ? (vpos >> 5) + 1 : 15], vpos & 31);
         uint32_t vb = vw & ((1u << B) - 1u);
         if (SGN) vb = (uint32_t)(((int32_t)(vb << (32 - B))) >> (32 - B)) & 0xFFu;
@@ -220,10 +227,10 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
       const uint4 o4 = O[0];
       v4n = Vg[0];
       f4n = __shfl_sync(0xFFFFFFFFu, Fg[0], 0);
-      Wn[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x + lane4));
-      Wn[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y + lane4));
-      Wn[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z + lane4));
-      Wn[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w + lane4));
+      Wn[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x * RB + lane4));
+      Wn[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y * RB + lane4));
+      Wn[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z * RB + lane4));
+      Wn[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w * RB + lane4));
     }
 #pragma unroll 2
     for (int g = 0; g < NG; g++) {
@@ -233,10 +240,10 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
         const uint4 o4 = O[g + 1];
         v4n = Vg[g + 1];
         f4n = __shfl_sync(0xFFFFFFFFu, Fg[g + 1], 0);
-        Wn[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x + lane4));
-        Wn[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y + lane4));
-        Wn[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z + lane4));
-        Wn[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w + lane4));
+        Wn[0] = *reinterpret_cast<const uint32_t*>(qtb + (o4.x * RB + lane4));
+        Wn[1] = *reinterpret_cast<const uint32_t*>(qtb + (o4.y * RB + lane4));
+        Wn[2] = *reinterpret_cast<const uint32_t*>(qtb + (o4.z * RB + lane4));
+        Wn[3] = *reinterpret_cast<const uint32_t*>(qtb + (o4.w * RB + lane4));
       }
       uint32_t V[4];
       transpose4(W, V);
@@ -300,10 +307,11 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
 template <int B, bool SGN, int MODE>
 __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  uint8_t* qtb = smem;                                           // [cols][128] bytes
-  uint32_t* thr_s = reinterpret_cast<uint32_t*>(smem + (size_t)a.cols * kBatchQ);
+  uint8_t* qtb = smem;                                           // [cols][33] words
+  const size_t qtab_bytes = batch_qtab_words(a.cols) * 4;
+  uint32_t* thr_s = reinterpret_cast<uint32_t*>(smem + qtab_bytes);
   const bool thr_in_smem = (MODE == MODE_FILTER) && batch_thr_in_smem(a.split);
-  unsigned char* wsm_all = smem + (size_t)a.cols * kBatchQ +
+  unsigned char* wsm_all = smem + qtab_bytes +
                            (batch_thr_in_smem(a.split) ? (size_t)a.split * kBatchQ * 4 : 0);
   // the warp index through a shuffle from lane 0: the compiler then treats the range bounds, and
   // every branch on them, as warp-uniform
@@ -319,7 +327,7 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
     const uint4* src = reinterpret_cast<const uint4*>(a.qtab);
     uint4* dst = reinterpret_cast<uint4*>(qtb);
     // eight independent loads per thread in flight: the fill is latency-bound otherwise
-    const uint32_t n = a.cols * (kBatchQ / 16);
+    const uint32_t n = (uint32_t)(qtab_bytes / 16);
     for (uint32_t i0 = 0; i0 < n; i0 += 8 * blockDim.x) {
       uint4 v[8];
 #pragma unroll
@@ -370,18 +378,21 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
   }
 }
 
-// qtab[col][32] words: byte t of word (col, l) = quantised query q0 + 4l + t at col (0 past nq)
+// qtab[col][33] words: byte t of word (col, l) = quantised query q0 + 4l + t at col (0 past nq);
+// word 32 of each column and the padding to a 16-byte slot are zero
 __global__ void k_qtable(const int8_t* __restrict__ q8, uint32_t ld8, uint32_t cols, uint32_t q0,
                          uint32_t nq, uint32_t* __restrict__ qtab) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cols * 32u) return;
-  const uint32_t c = i >> 5, l = i & 31u;
+  if (i >= batch_qtab_words(cols)) return;
+  const uint32_t c = i / kQtabWords, l = i % kQtabWords;
   uint32_t w = 0;
+  if (c < cols && l < 32u) {
 #pragma unroll
-  for (int t = 0; t < 4; t++) {
-    const uint32_t q = 4 * l + t;
-    const uint32_t b = q < nq ? (uint32_t)(uint8_t)q8[(size_t)(q0 + q) * ld8 + c] : 0u;
-    w |= b << (8 * t);
+    for (int t = 0; t < 4; t++) {
+      const uint32_t q = 4 * l + t;
+      const uint32_t b = q < nq ? (uint32_t)(uint8_t)q8[(size_t)(q0 + q) * ld8 + c] : 0u;
+      w |= b << (8 * t);
+    }
   }
   qtab[i] = w;
 }

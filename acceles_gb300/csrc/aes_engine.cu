@@ -176,7 +176,7 @@ struct Engine {
   int plain_grid = 0, smem_optin = 0;
   size_t plain_smem = 0, final_smem = 0;
   // batched pass
-  uint32_t* d_qtab = nullptr;     // [blocks][cols][32] words
+  uint32_t* d_qtab = nullptr;     // [blocks][batch_qtab_words(cols)] words
   int batch_warps_n = 0, batch_grid = 0;
   size_t batch_smem = 0;
   uint32_t batch_mode = 0;        // 0 auto, 1 never, else always
@@ -364,7 +364,7 @@ int Engine::plan_config(const aes_params& p, Config* c) const {
   plan += nblk * kBatchQ * (size_t)c->n_sample_rows * 4;
   plan += maxB * (ld32 * 4ull + ld8 + S * 8ull + (size_t)S * c->cap * 8 + c->nslots * 8ull + 4 +
                   p.k_max * 8ull);
-  plan += nblk * cols * 128;
+  plan += nblk * batch_qtab_words(cols) * 4;
   plan += p.k_max * 8ull;
   c->plan = plan;
 
@@ -406,7 +406,7 @@ int Engine::apply_config(const Config& c) {
   AES_AL(d_status, maxB);
   AES_AL(d_out_idx, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
-  AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * cols * 32);
+  AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * batch_qtab_words(cols));
   AES_AL(d_exact_cand, std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_exact_key, std::max<uint32_t>(p.k_max, 1));
 #undef AES_AL
@@ -638,7 +638,7 @@ int Engine::run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
   a.n_tiles = (uint32_t)tiles;
   a.n_rows = rows;
   a.cols = cols;
-  a.qtab = d_qtab + (size_t)blk * cols * 32;
+  a.qtab = d_qtab + (size_t)blk * batch_qtab_words(cols);
   a.q0 = blk * kBatchQ;
   a.nq = nq_blk;
   a.rowscale = d_rowscale;
@@ -696,8 +696,8 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   if (batched) {
     for (uint32_t b = 0; b < nblk; b++) {
       const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
-      k_qtable<<<(cols * 32 + 255) / 256, 256, 0, s>>>(d_q8, ld8, cols, b * kBatchQ, nb,
-                                                       d_qtab + (size_t)b * cols * 32);
+      k_qtable<<<(uint32_t)((batch_qtab_words(cols) + 255) / 256), 256, 0, s>>>(
+          d_q8, ld8, cols, b * kBatchQ, nb, d_qtab + (size_t)b * batch_qtab_words(cols));
       AES_CK(cudaGetLastError());
       n_launch++;
       int rc = run_batch(MODE_SAMPLE, b, nb, s);
