@@ -149,6 +149,42 @@ struct BatchRows {
     }
   }
 
+  // key threshold of partition p for this lane's query t
+  __device__ __forceinline__ uint32_t thr_q(uint32_t p, int t) const {
+    if (a.split <= 1) return thr4[t];
+    if (thr_s) return thr_s[p * kBatchQ + 4 * lane + t];
+    const uint32_t q = 4 * lane + t;
+    return q < a.nq ? __ldg(a.thr + (size_t)(a.q0 + q) * a.split + p) : 0xFFFFFFFFu;
+  }
+  // integer keys: per query, the lowest score bound over the partitions of rows r0 .. r1 (one
+  // partition for almost every tile: the partitions are contiguous row ranges)
+  __device__ __forceinline__ void bounds(uint32_t r0, uint32_t r1, int32_t (&b)[4]) const {
+    if (a.split <= 1) {
+#pragma unroll
+      for (int t = 0; t < 4; t++) b[t] = thr_sc[t];
+      return;
+    }
+#pragma unroll
+    for (int t = 0; t < 4; t++) b[t] = 0x7FFFFFFF;
+    const uint32_t p1 = part_of(r1, a.split, a.slice);
+    for (uint32_t p = part_of(r0, a.split, a.slice); p <= p1; p++) {
+#pragma unroll
+      for (int t = 0; t < 4; t++) b[t] = min(b[t], (int32_t)(thr_q(p, t) ^ 0x80000000u));
+    }
+  }
+  // integer keys: row `row` finished with scores acc[0..3]; bound b from bounds()
+  __device__ __forceinline__ void finish_int(uint32_t row, const int32_t (&acc)[4],
+                                             const int32_t (&b)[4]) const {
+    const bool hit = (acc[0] >= b[0]) | (acc[1] >= b[1]) | (acc[2] >= b[2]) | (acc[3] >= b[3]);
+    if (__ballot_sync(0xFFFFFFFFu, hit)) {
+      const uint32_t p = part_of(row, a.split, a.slice);
+      uint32_t th[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) th[t] = thr_q(p, t);
+      append(row, p, acc, th, false);
+    }
+  }
+
   // survivors of a finished row (rare): v[t] is the key (is_key) or the integer score
   __device__ __forceinline__ void append(uint32_t row, uint32_t p, const int32_t (&v)[4],
                                       const uint32_t (&th)[4], bool is_key) const {
@@ -192,6 +228,18 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
     }
     const bool closing = (t >= te);
     bool simple = owned && !closing;  // boundaries need neither the ownership nor the end test
+    // integer keys: compare against the tile's per-query score bounds, exact check on a hit
+    constexpr bool kIntKeysPossible = MODE == MODE_FILTER;
+    const bool intk = kIntKeysPossible && !a.rowscale;
+    int32_t bnd[4] = {0, 0, 0, 0};
+    if (intk) {
+      const uint32_t nfl = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)popc_flags(PacketDecoder<B, SGN>::flags(w)));
+      rows.bounds(row, row + nfl, bnd);
+    }
+    auto fin = [&](uint32_t r, const int32_t (&x)[4]) {
+      if (kIntKeysPossible && intk) rows.finish_int(r, x, bnd);
+      else rows.finish(r, x);
+    };
     // prefetch one tile ahead up to the first closing tile; later tiles are read on demand
     if (t + 1 <= te && t + 1 < a.n_tiles) load_tile(a.tiles, t + 1, lane, nw);
     // ---- phase A: this lane's packet -> records ----------------------------------------------
@@ -262,11 +310,11 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(hi, V[q], 0);
         if (simple) {  // an owned row inside the range
-          rows.finish(row, s);
+          fin(row, s);
           row++;
           continue;
         }
-        if (owned) rows.finish(row, s);
+        if (owned) fin(row, s);
         if (closing) return;
         row++;
         owned = true;
@@ -282,7 +330,7 @@ __device__ void batch_range(const BatchArgs& a, uint32_t tb, uint32_t te,
         const uint32_t m = lo_mask & ~(0xFFFFFFFFu << (8 * i));  // bytes [lo, i)
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[q] = dot4<SGN>(v4 & m, V[q], acc[q]);
-        if (owned) rows.finish(row, acc);
+        if (owned) fin(row, acc);
         if (closing) return;
         row++;
         owned = true;

@@ -114,6 +114,29 @@ struct Emitter {
     const uint32_t i = atomicAdd(a.cnt, 1u);
     if (i < a.cap) a.surv[i] = make_uint2(key_i32(score), row);
   }
+  // filter with integer keys (no row scales), any number of partitions
+  __device__ __forceinline__ bool int_keys() const { return MODE == MODE_FILTER && !a.rowscale; }
+  __device__ __forceinline__ uint32_t thr_of(uint32_t p) const {
+    return a.split <= 1 ? thr0 : (a.split <= kThrSmemMax ? thr_s[p] : __ldg(a.thr + p));
+  }
+  // the lowest score bound over the partitions of rows r0 .. r1 (one partition for almost every
+  // tile: the partitions are contiguous row ranges)
+  __device__ __forceinline__ int32_t score_bound(uint32_t r0, uint32_t r1) const {
+    if (a.split <= 1) return thr_score();
+    const uint32_t p1 = part_of(r1, a.split, a.slice);
+    int32_t b = 0x7FFFFFFF;
+    for (uint32_t p = part_of(r0, a.split, a.slice); p <= p1; p++)
+      b = min(b, (int32_t)(thr_of(p) ^ 0x80000000u));
+    return b;
+  }
+  // a row whose integer score passed a bound: kept if it passes its own partition's threshold
+  __device__ __forceinline__ void append_checked(uint32_t row, int32_t score) const {
+    const uint32_t p = part_of(row, a.split, a.slice);
+    if (score >= (int32_t)(thr_of(p) ^ 0x80000000u)) {
+      const uint32_t i = atomicAdd(a.cnt + p, 1u);
+      if (i < a.cap) a.surv[(size_t)p * a.cap + i] = make_uint2(key_i32(score), row);
+    }
+  }
   __device__ __forceinline__ void operator()(uint32_t row, int32_t score) const {
     uint32_t key;
     if (a.rowscale) key = key_f32(__fmul_rn(__int2float_rn(score), __ldg(a.rowscale + row)));
@@ -447,14 +470,27 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32
   return false;
 }
 
-// One tile of a warp's range (B = 8).  Returns true once the range is complete.  INTF: the
-// integer filter with one partition, a compare per row and the survivor append only on a hit.
-// CLOSING: a tile at or past the range's end, where only the first flag matters.
-template <bool SGN, int MODE, bool INTF, bool CLOSING>
+// How a plain pass emits rows: any emitter, or the filter with integer keys (no row scales) and
+// one partition, or with several partitions.
+enum EmitKind : int { EMIT_ANY = 0, EMIT_INT_ONE = 1, EMIT_INT_PARTS = 2 };
+
+// The partition of a warp's current tile, followed across tiles without a division.
+struct PartTrack {
+  uint32_t p;    // partition of the tile's first row
+  uint32_t end;  // first row of partition p + 1 (0xFFFFFFFF: p is the last)
+  int32_t ts;    // score bound of partition p
+};
+
+// One tile of a warp's range (B = 8).  Returns true once the range is complete.
+// KIND EMIT_INT_*: a compare per row against the score bound of the partition of the tile's rows
+// (the lowest over its partitions when it straddles some), and the exact check and survivor
+// append only on a hit.  CLOSING: a tile at or past the range's end, where only the first flag
+// matters.
+template <bool SGN, int MODE, int KIND, bool CLOSING>
 __device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
                                            const uint32_t (&w)[16], uint32_t rowbase,
                                            RangeState& st, const Emitter<MODE>& emit,
-                                           const char* qtb) {
+                                           const char* qtb, PartTrack& pt) {
   using D = Packet8<SGN>;
   const uint32_t lane = threadIdx.x & 31u;
   if constexpr (CLOSING) {
@@ -466,14 +502,27 @@ __device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
   const uint32_t F = w[0] & ((1u << D::P) - 1u);
   const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
   uint32_t rbase = rowbase;  // row closed by this lane's first flag
+  int32_t ts = 0;            // EMIT_INT_*: score bound of the rows this tile closes
   if constexpr (!CLOSING) {
     const uint32_t nf = __popc(F);
-    rbase += warp_incl_sum(nf, lane) - nf;
+    const uint32_t incl = warp_incl_sum(nf, lane);
+    rbase += incl - nf;
+    if constexpr (KIND == EMIT_INT_ONE) ts = emit.thr_score();
+    if constexpr (KIND == EMIT_INT_PARTS) {
+      const uint32_t r1 = rowbase + __shfl_sync(0xFFFFFFFFu, incl, 31);
+      while (rowbase >= pt.end) {  // the tile starts in a later partition
+        pt.p++;
+        pt.end = (pt.p + 1 >= a.split) ? 0xFFFFFFFFu : pt.end + a.slice;
+        pt.ts = (int32_t)(emit.thr_of(pt.p) ^ 0x80000000u);
+      }
+      ts = r1 < pt.end ? pt.ts : emit.score_bound(rowbase, r1);
+    }
   }
-  const int32_t ts = emit.thr_score();
   auto on_row = [&](bool valid, uint32_t row, int32_t sc) {
-    if constexpr (INTF) {
+    if constexpr (KIND == EMIT_INT_ONE) {
       if (valid && sc >= ts) emit.append_int(row, sc);
+    } else if constexpr (KIND == EMIT_INT_PARTS) {
+      if (valid && sc >= ts) emit.append_checked(row, sc);
     } else {
       if (valid) emit(row, sc);
     }
@@ -516,12 +565,19 @@ __device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
 // and later reads back, only its own 64 bytes, so no synchronisation between lanes is needed.
 // Tiles up to te (the first closing tile) are fetched one ahead; tiles past te only when the open
 // row runs on through the closing tile.
-template <int B, bool SGN, int MODE, bool INTF>
+template <int B, bool SGN, int MODE, int KIND>
 __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
                            const Emitter<MODE>& emit, const char* qtb, uint4* E4, uint4* stg) {
   const uint32_t lane = threadIdx.x & 31u;
   if (tb >= te) return;
   RangeState st{tb == 0, 0u, 0u};  // row 0 starts at entry 0 without a flag
+  PartTrack pt{0u, 0xFFFFFFFFu, 0};
+  if constexpr (KIND == EMIT_INT_PARTS) {
+    const uint32_t r0 = __ldg(a.tile_rowbase + tb);
+    pt.p = part_of(r0, a.split, a.slice);
+    pt.end = (pt.p + 1 >= a.split || a.slice == 0) ? 0xFFFFFFFFu : (pt.p + 1) * a.slice;
+    pt.ts = (int32_t)(emit.thr_of(pt.p) ^ 0x80000000u);
+  }
   uint32_t w[16];
   uint32_t rn = 0;
   auto fetch = [&](uint32_t t) {
@@ -552,8 +608,8 @@ __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
     if (t + 1 <= te) fetch(t + 1);
     if constexpr (B == 8) {
       if (t < te) {  // te <= n_tiles
-        tile_step8<SGN, MODE, INTF, false>(a, t, w, r, st, emit, qtb);
-      } else if (tile_step8<SGN, MODE, INTF, true>(a, t, w, r, st, emit, qtb)) {
+        tile_step8<SGN, MODE, KIND, false>(a, t, w, r, st, emit, qtb, pt);
+      } else if (tile_step8<SGN, MODE, KIND, true>(a, t, w, r, st, emit, qtb, pt)) {
         return;
       }
     } else {
@@ -625,19 +681,20 @@ __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a)
     for (uint32_t s = gw; s < a.n_sample_tiles; s += nw) {
       const uint32_t t = s * a.sample_stride;
       Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s)};
-      cand_range<B, SGN, MODE, false>(a, t, t + 1, em, qtb, E4, stg);
+      cand_range<B, SGN, MODE, EMIT_ANY>(a, t, t + 1, em, qtb, E4, stg);
     }
   } else {
     const uint64_t n = a.n_tiles;
     const uint32_t tb = (uint32_t)((n * gw) / nw), te = (uint32_t)((n * (gw + 1)) / nw);
     Emitter<MODE> em{a, thr_s, thr0, 0u};
     if constexpr (B == 8 && MODE == MODE_FILTER) {
-      if (em.int_filter()) {
-        cand_range<B, SGN, MODE, true>(a, tb, te, em, qtb, E4, stg);
+      if (em.int_keys()) {
+        if (a.split <= 1) cand_range<B, SGN, MODE, EMIT_INT_ONE>(a, tb, te, em, qtb, E4, stg);
+        else cand_range<B, SGN, MODE, EMIT_INT_PARTS>(a, tb, te, em, qtb, E4, stg);
         return;
       }
     }
-    cand_range<B, SGN, MODE, false>(a, tb, te, em, qtb, E4, stg);
+    cand_range<B, SGN, MODE, EMIT_ANY>(a, tb, te, em, qtb, E4, stg);
   }
 }
 

@@ -175,6 +175,8 @@ def main():
     ap.add_argument("--no-gpu-baseline", action="store_true")
     ap.add_argument("--check", type=int, default=2, help="queries checked against the oracle")
     ap.add_argument("--rows", type=int, default=ROWS, help="smaller matrix, for profiling only")
+    ap.add_argument("--split", type=int, default=1,
+                    help="row partitions with a Top-(CK/split) each (the reference default is 32)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -244,7 +246,7 @@ def main():
             ms = float(t.item())
         return ms, st, repaired, clk, Qh
 
-    common = dict(bits=BITS, quant=E.QUANT_SYM_GLOBAL, split=1, ck=CK, k_max=K, device=local,
+    common = dict(bits=BITS, quant=E.QUANT_SYM_GLOBAL, split=args.split, ck=CK, k_max=K, device=local,
                   flags=E.FLAG_PROFILE)
     # plain: one candidate pass per query
     Bp = args.batch
@@ -311,7 +313,7 @@ def main():
         ri, rs = eng.read_topk()
         recalls, exact = [], True
         for i in range(min(args.check, B)):
-            oi, os_, _ = m.two_stage(Qh[i], 1, CK, K)
+            oi, os_, _ = m.two_stage(Qh[i], args.split, CK, K)
             exact &= bool(np.array_equal(ri[i], oi)) and bool(np.array_equal(rs[i], os_))
             f64 = orc.scores_f64(m.ptr, m.col, m.val, Qh[i], rows)
             top = np.argsort(-f64, kind="stable")[:K]
@@ -328,8 +330,9 @@ def main():
             "ms_per_step": ms / args.steps_batched,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded; reference matrices not shipped)",
-            "config": {"workload": f"{rows // 1_000_000}Mx1024 deg U{{10..30}} U(0,1), 8-bit Ultra-CSR, CK=1024, K=100, split=1",
+            "config": {"workload": f"{rows // 1_000_000}Mx1024 deg U{{10..30}} U(0,1), 8-bit Ultra-CSR, CK=1024, K=100, split={args.split}",
                        "rows": rows, "cols": COLS, "nnz": info["nnz"], "bits": BITS, "ck": CK,
+                       "split": args.split,
                        "k": K, "batch": Bb, "path": "batched (one candidate pass per 128 queries)",
                        "plain_batch": Bp, "plain_steps": args.steps,
                        "parallelism": f"replicas x{world}",

@@ -67,6 +67,19 @@ def test_two_stage_matches_oracle(bits, quant, split, ck):
     check_run(m, eng, queries(cols, 3, 1, signed=(quant == 0)), split, ck, k)
 
 
+@pytest.mark.parametrize("split,ck,nq,bt", [(32, 1024, 3, 1), (32, 1024, 40, 128),
+                                            (2000, 4000, 3, 1), (600, 1200, 20, 128)])
+def test_partition_bounds_per_tile(split, ck, nq, bt):
+    """Integer keys with many row partitions: the candidate passes compare each row with the
+    lowest threshold of the partitions its tile touches and check a hit against its own
+    partition.  Short slices make tiles straddle several partitions; 600 and 2000 partitions
+    keep their thresholds in global memory."""
+    rows, cols, k = 20000, 1024, 100
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 31, 8, 0, split, ck, k, nq=nq,
+                  batch_tile=bt)
+    check_run(m, eng, queries(cols, nq, 5, signed=True), split, ck, k)
+
+
 def test_config1_shape_absnormal_b6_split32():
     # 400k x 500 at 69 nnz/row in the reference, here scaled down; queries = densified rows
     rows, cols = 12800, 500
@@ -203,6 +216,29 @@ def test_batched_matches_oracle(bits, quant, split, ck, nq):
     idx, sc = eng.read_topk()
     for i in range(0, nq, max(1, nq // 9)):
         oi, os_, cand = m.two_stage(Q[i], split, ck, k)
+        n = len(oi)
+        assert np.array_equal(idx[i, :n], oi), i
+        assert np.array_equal(sc[i, :n], os_), i
+        gi, _, _ = eng.read_candidates(i)
+        keys = m.keys(Q[i])
+        exp = cand[np.lexsort((-cand.astype(np.int64), -keys[cand].astype(np.int64)))]
+        assert np.array_equal(gi, exp), i
+
+
+@pytest.mark.parametrize("bits,lo,hi", [(8, 1, 5), (8, 3, 14), (8, 9, 11), (4, 2, 9),
+                                         (6, 1, 3)])
+def test_batched_short_rows(bits, lo, hi):
+    """Rows of a few entries: a tile whose rows, each padded to a multiple of four entries, no
+    longer fit the per-warp records keeps the unpadded walk, so one pass mixes both layouts."""
+    rows, cols, k, nq = 30000, 512, 50, 130
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, lo, hi, 40 + lo, bits, 0, 4, 256, k, nq=nq,
+                  batch_tile=128)
+    Q = queries(cols, nq, 19, signed=True)
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    for i in range(0, nq, 11):
+        oi, os_, cand = m.two_stage(Q[i], 4, 256, k)
         n = len(oi)
         assert np.array_equal(idx[i, :n], oi), i
         assert np.array_equal(sc[i, :n], os_), i
