@@ -255,7 +255,7 @@ struct Engine {
                     cudaStream_t s);
   int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
              uint32_t* repaired);
-  int run_plain(int mode, uint32_t q, cudaStream_t s);
+  int run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y = 1);
   int run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s);
   int collect_profile();
 };
@@ -580,7 +580,8 @@ int Engine::retune(const aes_params& p) {
   return AES_OK;
 }
 
-int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
+// mode's pass for query q (MODE_SAMPLE: for queries q .. q + nq_y - 1 in one launch)
+int Engine::run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y) {
   PlainArgs a{};
   a.tiles = d_tiles;
   a.tile_rowbase = d_tile_rowbase;
@@ -600,9 +601,17 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
   a.n_sample_tiles = n_sample_tiles;
   if (mode == MODE_SAMPLE) a.keys_out = d_sample_keys + (size_t)q * n_sample_rows;
   else if (mode == MODE_ALL) a.keys_out = d_allkeys;
+  if (mode != MODE_SAMPLE) nq_y = 1;
+  a.q8_ld = (uint32_t)ld8;
+  a.keys_ld = (uint32_t)n_sample_rows;
   int grid = plain_grid;
   const int pw = plain_warps((int)bits);
-  if (mode == MODE_SAMPLE) grid = std::min<int>(grid, (int)((n_sample_tiles + pw - 1) / pw));
+  if (mode == MODE_SAMPLE) {
+    // one warp per sample tile for a single query; for several, about two waves of CTAs in all,
+    // each warp taking several tiles, so the query table is filled fewer times
+    grid = std::min<int>(grid, (int)((n_sample_tiles + pw - 1) / pw));
+    if (nq_y > 1) grid = std::min<int>(grid, (int)((2u * (uint32_t)sm_count + nq_y - 1) / nq_y));
+  }
   grid = std::max(grid, 1);
   const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
   if (prof) {
@@ -620,7 +629,7 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s) {
     }
     AES_CK(cudaEventRecord(prof_ev[prof_used], s));
   }
-  pick_plain((int)bits, sgn, mode)<<<grid, plain_threads((int)bits), plain_smem, s>>>(a);
+  pick_plain((int)bits, sgn, mode)<<<dim3(grid, nq_y), plain_threads((int)bits), plain_smem, s>>>(a);
   AES_CK(cudaGetLastError());
   if (prof) {
     AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
@@ -704,8 +713,8 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
       if (rc) return rc;
     }
   } else {
-    for (uint32_t q = 0; q < nq; q++) {
-      int rc = run_plain(MODE_SAMPLE, q, s);
+    for (uint32_t q0 = 0; q0 < nq; q0 += 65535u) {  // every query's sample pass in one launch
+      int rc = run_plain(MODE_SAMPLE, q0, s, std::min<uint32_t>(65535u, nq - q0));
       if (rc) return rc;
     }
   }

@@ -86,6 +86,9 @@ struct PlainArgs {
   uint32_t* keys_out;           // MODE_SAMPLE: [sample rows]; MODE_ALL: [n_rows]
   const uint32_t* sample_first; // MODE_SAMPLE: owned-row offset per sample tile
   uint32_t sample_stride, n_sample_tiles;
+  // MODE_SAMPLE over several queries in one launch: query blockIdx.y reads q8 + y * q8_ld and
+  // writes its keys at keys_out + y * keys_ld
+  uint32_t q8_ld, keys_ld;
 };
 
 constexpr uint32_t kThrSmemMax = 1024;  // thresholds of up to this many partitions in smem
@@ -652,7 +655,8 @@ __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a)
   // replicate the query once per lane; the bytes are staged through the (not yet used) area
   // after the table so the fill needs one global round trip
   int8_t* qstage = reinterpret_cast<int8_t*>(after);
-  for (uint32_t i = threadIdx.x; i < a.cols; i += blockDim.x) qstage[i] = a.q8[i];
+  const int8_t* q8 = a.q8 + (size_t)blockIdx.y * a.q8_ld;
+  for (uint32_t i = threadIdx.x; i < a.cols; i += blockDim.x) qstage[i] = q8[i];
   __syncthreads();
   if constexpr (B == 8) {
     uint4* qt = reinterpret_cast<uint4*>(smem);  // four lane copies per store
@@ -680,7 +684,8 @@ __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a)
   if constexpr (MODE == MODE_SAMPLE) {
     for (uint32_t s = gw; s < a.n_sample_tiles; s += nw) {
       const uint32_t t = s * a.sample_stride;
-      Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s)};
+      // keys of query y land keys_ld further on: the index row - base wraps to that offset
+      Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s) - blockIdx.y * a.keys_ld};
       cand_range<B, SGN, MODE, EMIT_ANY>(a, t, t + 1, em, qtb, E4, stg);
     }
   } else {
