@@ -24,9 +24,9 @@
 namespace aes {
 namespace dev {
 
-// warps per CTA of the plain candidate pass: as many as the query table, each warp's prefix
-// staging and next-tile buffer, and the partition thresholds leave room for in 227 KB
-__host__ __device__ constexpr int plain_warps(int B) { return B == 8 ? 32 : (B == 6 ? 26 : 24); }
+// warps per CTA of the plain candidate pass: 32 (the 128 KB query table and 32 next-tile buffers
+// of 2 KB leave room for the partition thresholds in 227 KB)
+__host__ __device__ constexpr int plain_warps(int) { return 32; }
 __host__ __device__ constexpr int plain_threads(int B) { return plain_warps(B) * 32; }
 
 enum Mode : int { MODE_FILTER = 0, MODE_SAMPLE = 1, MODE_ALL = 2 };
@@ -108,9 +108,6 @@ struct Emitter {
   uint32_t thr0;          // threshold when split == 1
   uint32_t sample_base;   // MODE_SAMPLE: first owned row minus its key index
   // filter with integer keys and one partition: key >= thr0 <=> score >= thr0 ^ 0x80000000
-  __device__ __forceinline__ bool int_filter() const {
-    return MODE == MODE_FILTER && !a.rowscale && a.split <= 1;
-  }
   __device__ __forceinline__ int32_t thr_score() const { return (int32_t)(thr0 ^ 0x80000000u); }
   // a row of the integer filter whose score passed thr_score()
   __device__ __forceinline__ void append_int(uint32_t row, int32_t score) const {
@@ -184,54 +181,11 @@ __device__ __forceinline__ uint32_t window32(const uint32_t (&w)[16]) {
   else return __funnelshift_r(w[k], w[k + 1], s);
 }
 
-// Per-lane decode of one B = 4 or 6 packet.  Element j: 10-bit column at bit P + 10j, B-bit
-// value at bit 11P + Bj (fpga_utils.hpp:349-384).  run() returns the packet's sum of
-// val_i * q[col_i] (int32, wrapping) and stages the running sum S_j of every entry, four per
-// 16-byte slot, from which prefix() gives the running sum before any entry.
+// The flag word of a packet: bit j set when entry j starts a row (fpga_utils.hpp:349-384).
 template <int B, bool SGN>
 struct PacketDecoder {
   static constexpr int P = packet_elems(B);
   using Flags = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
-
-  // q[col_J] from the lane-replicated table qt[col][32] (int16): the column window starts 6
-  // bits early so (col << 6), the row offset of col in the table, lands at bits 6..15
-  template <int J>
-  __device__ __forceinline__ static int32_t qval(const uint32_t (&w)[16], const char* qtb,
-                                                 uint32_t lane2) {
-    const uint32_t y = window32<P + 10 * J - 6>(w);
-    return *reinterpret_cast<const int16_t*>(qtb + ((y & 0xFFC0u) | lane2));
-  }
-
-  template <int J>
-  __device__ __forceinline__ static void step(const uint32_t (&w)[16], const char* qtb,
-                                              uint32_t lane2, uint4* E4, int32_t& S,
-                                              int32_t (&s4)[4]) {
-    if constexpr (J < P) {
-      const int32_t q = qval<J>(w, qtb, lane2);
-      const uint32_t z = window32<11 * P + B * J + B - 32>(w);  // value in the top B bits
-      const int32_t v = SGN ? ((int32_t)z >> (32 - B)) : (int32_t)(z >> (32 - B));
-      S += v * q;
-      s4[J & 3] = S;
-      if constexpr ((J & 3) == 3 || J == P - 1)
-        E4[(J >> 2) * 32] = make_uint4((uint32_t)s4[0], (uint32_t)s4[1], (uint32_t)s4[2], (uint32_t)s4[3]);
-      step<J + 1>(w, qtb, lane2, E4, S, s4);
-    }
-  }
-
-  __device__ __forceinline__ static int32_t run(const uint32_t (&w)[16], const char* qtb,
-                                                uint32_t lane2, uint4* E4) {
-    int32_t S = 0;
-    int32_t s4[4] = {0, 0, 0, 0};
-    step<0>(w, qtb, lane2, E4, S, s4);
-    return S;
-  }
-
-  // running sum of this lane's packet before entry j (0 for j == 0)
-  __device__ __forceinline__ static uint32_t prefix(const uint32_t* Ew, uint32_t lane, int j) {
-    if (j == 0) return 0u;
-    const int i = j - 1;
-    return Ew[(((i >> 2) * 32 + lane) << 2) | (i & 3)];
-  }
 
   __device__ __forceinline__ static Flags flags(const uint32_t (&w)[16]) {
     if constexpr (P <= 32) {
@@ -242,12 +196,13 @@ struct PacketDecoder {
   }
 };
 
-// Per-lane decode of one B = 8 packet (26 entries, same field layout).  Four consecutive values
-// are one 32-bit window, so a group of four entries is one dp4a of the packed values with the
-// four query bytes.  A row that starts and ends inside the packet is scored while the groups
-// are decoded: the running sum at a flag is the sum before its group plus a dp4a of the bytes
-// before it.  Nothing is staged in shared memory; only the row closed by a lane's first flag
-// needs the running sums of the lanes before it, which the warp scan gives after the decode.
+// Per-lane decode of one packet in spans.  Element j: 10-bit column at bit P + 10j, B-bit value
+// at bit 11P + Bj (fpga_utils.hpp:349-384).  A group of four entries is one dp4a of its four
+// values (unpacked to bytes in element order) with the four query bytes.  A row that starts and
+// ends inside the packet is scored while the groups are decoded: the running sum at a flag is
+// the sum before its span plus a dp4a of the bytes before it.  Nothing is staged in shared
+// memory; only the row closed by a lane's first flag needs the running sums of the lanes before
+// it, which the warp scan gives after the decode.
 struct Rows8 {
   int32_t S;       // running sum of the packet so far
   uint32_t first;  // running sum before the first flagged entry
@@ -256,10 +211,11 @@ struct Rows8 {
   bool seen;       // a flag was met
 };
 
-template <bool SGN>
-struct Packet8 {
-  static constexpr int P = packet_elems(8);
+template <int B, bool SGN>
+struct PacketSpans {
+  static constexpr int P = packet_elems(B);
   static constexpr int NG = (P + 3) / 4;
+  using Flags = typename PacketDecoder<B, SGN>::Flags;
 
   // q[col_J] from the lane-replicated 32-bit table qt[col][32]: lane l reads bank l whatever the
   // columns, so a gather is one wavefront.  The column window starts 7 bits early so
@@ -275,6 +231,32 @@ struct Packet8 {
     return SGN ? __dp4a((int)v4, (int)q4, c) : (int32_t)__dp4a(v4, q4, (unsigned)c);
   }
 
+  // bits [POS, POS + 32) of the packet, or, near its end, the 32 bits ending at bit 512 shifted
+  // down so that bit POS comes first (the bits above the packet's end read as zero)
+  template <int POS>
+  __device__ __forceinline__ static uint32_t field32(const uint32_t (&w)[16]) {
+    if constexpr (POS + 32 <= 512) return window32<POS>(w);
+    else return window32<480>(w) >> (POS - 480);
+  }
+
+  // the four B-bit values at the bottom of x as bytes in element order (sign-extended when SGN)
+  __device__ __forceinline__ static uint32_t unpack(uint32_t x) {
+    if constexpr (B == 8) {
+      return x;
+    } else if constexpr (B == 4) {
+      const uint32_t z = __byte_perm(x, 0u, 0x4140);  // entries 0,1 | 0 | entries 2,3 | 0
+      uint32_t v = (z | (z * 16u)) & 0x0F0F0F0Fu;
+      if constexpr (SGN) v |= (v & 0x08080808u) * 0x1Eu;  // bit 3 -> bits 4..7 of each byte
+      return v;
+    } else {
+      static_assert(B == 6, "bit width");
+      const uint32_t h = (x & 0xFFFu) | ((x * 16u) & 0x0FFF0000u);      // 12-bit halves
+      uint32_t v = (h & 0x003F003Fu) | ((h * 4u) & 0x3F003F00u);        // 6-bit bytes
+      if constexpr (SGN) v |= (v & 0x20202020u) * 6u;  // bit 5 -> bits 6..7 of each byte
+      return v;
+    }
+  }
+
   // q0..q3 of group G packed into one word, and its four values
   template <int G>
   __device__ __forceinline__ static void load_group(const uint32_t (&w)[16], const char* qtb,
@@ -287,13 +269,12 @@ struct Packet8 {
     if constexpr (n > 1) q4 += qval<(n > 1 ? J + 1 : J)>(w, qtb, lane4) * 0x100u;
     if constexpr (n > 2) q4 += qval<(n > 2 ? J + 2 : J)>(w, qtb, lane4) * 0x10000u;
     if constexpr (n > 3) q4 += qval<(n > 3 ? J + 3 : J)>(w, qtb, lane4) * 0x1000000u;
-    v4 = window32<11 * P + 32 * G>(w);
+    v4 = unpack(field32<11 * P + B * J>(w));
     if constexpr (n < 4) v4 &= (1u << (8 * n)) - 1u;
   }
 
-  // decode groups G .. G + NGR - 1 (eight entries, or the last ten) and score the rows closed by
-  // their flags (on_row(row, score) when inner).  The running sum at flag j of the span is the
-  // sum before the span plus the dp4a of the bytes before j, masked out of the packed values.
+  // The running sum at flag j of the span starting at group G (NGR groups): the sum before the
+  // span plus the dp4a of the bytes before j, masked out of the packed values.
   template <int G, int NGR>
   __device__ __forceinline__ static uint32_t span_prefix(int j, int32_t Sa, uint32_t qa,
                                                          uint32_t va, uint32_t qb, uint32_t vb,
@@ -311,34 +292,39 @@ struct Packet8 {
     }
   }
 
-  // flag bits of entries [4G, 4G + 4 * NGR) of the packet, for the span starting at group G
+  // Spans of two groups (eight entries); the last takes a short tail group as a third
+  // (B = 8: 8/8/10 entries, B = 6: 8/8/8/6, B = 4: 8/8/8/10).
   template <int G>
   __host__ __device__ static constexpr int span_groups() { return (G + 3 == NG) ? 3 : 2; }
+  // flag bits of the span starting at group G, in place
   template <int G>
-  __host__ __device__ static constexpr uint32_t span_bits() {
-    return ((P - 4 * G) < 4 * span_groups<G>() ? ((1u << (P - 4 * G)) - 1u)
-                                               : ((1u << (4 * span_groups<G>())) - 1u))
+  __host__ __device__ static constexpr uint64_t span_bits() {
+    return ((P - 4 * G) < 4 * span_groups<G>() ? ((1ull << (P - 4 * G)) - 1ull)
+                                               : ((1ull << (4 * span_groups<G>())) - 1ull))
            << (4 * G);
   }
-  // true when some span of this packet holds two or more flags (a row shorter than a span)
-  __device__ __forceinline__ static bool two_in_a_span(uint32_t F) {
-    constexpr uint32_t m0 = span_bits<0>(), m1 = span_bits<2>(), m2 = span_bits<4>();
-    static_assert((m0 | m1 | m2) == (1u << P) - 1u && NG == 7, "span layout");
-    const uint32_t a = F & m0, b = F & m1, c = F & m2;
-    return ((a & (a - 1u)) | (b & (b - 1u)) | (c & (c - 1u))) != 0u;
+  // true when some span from group G on holds two or more flags (a row shorter than a span)
+  template <int G = 0>
+  __device__ __forceinline__ static bool two_in_a_span(Flags F) {
+    if constexpr (G >= NG) {
+      return false;
+    } else {
+      const Flags f = F & (Flags)span_bits<G>();
+      return (f & (f - 1)) != 0 || two_in_a_span<G + span_groups<G>()>(F);
+    }
   }
 
   // Decode the span starting at group G and score the rows closed by its flags: each closed row
   // goes to on_row(valid, row, score) (INNER: not on the closing tile).  The lowest flag of the
-  // span is handled without a branch; further flags (MULTI: some lane of the warp has them) in
+  // span is handled without a branch; further flags (multi: some lane of the warp has them) in
   // a loop.
   template <int G, bool INNER, class OnRow>
   __device__ __forceinline__ static void span(const uint32_t (&w)[16], const char* qtb,
-                                              uint32_t lane4, uint32_t F, bool multi, Rows8& s,
+                                              uint32_t lane4, Flags F, bool multi, Rows8& s,
                                               const OnRow& on_row) {
     if constexpr (G < NG) {
       constexpr int NGR = span_groups<G>();
-      static_assert(NGR == 3 || G + 2 < NG, "span layout");
+      static_assert(G + NGR <= NG, "span layout");
       uint32_t qa, va, qb, vb, qc = 0u, vc = 0u;
       load_group<G>(w, qtb, lane4, qa, va);
       load_group<G + 1>(w, qtb, lane4, qb, vb);
@@ -346,7 +332,7 @@ struct Packet8 {
       const int32_t Sa = s.S;
       s.S = dot4(vb, qb, dot4(va, qa, Sa));
       if constexpr (NGR == 3) s.S = dot4(vc, qc, s.S);
-      const uint32_t fP = (F & span_bits<G>()) >> (4 * G);
+      const uint32_t fP = (uint32_t)((F & (Flags)span_bits<G>()) >> (4 * G));
       const bool has = fP != 0;
       const uint32_t Pj = span_prefix<G, NGR>(__ffs(fP) - 1, Sa, qa, va, qb, vb, qc, vc);
       if constexpr (INNER) on_row(has && s.seen, s.row, (int32_t)(Pj - s.prev));
@@ -397,82 +383,6 @@ struct RangeState {
   uint32_t carryG;  // running sum before the current tile
 };
 
-// One tile of a warp's range (B = 4, 6).  Returns true once the range is complete.
-template <int B, bool SGN, int MODE>
-__device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t, uint32_t te,
-                                          const uint32_t (&w)[16], uint32_t rowbase,
-                                          RangeState& st, const Emitter<MODE>& emit,
-                                          const char* qtb, uint4* E4) {
-  using D = PacketDecoder<B, SGN>;
-  using Flags = typename D::Flags;
-  const uint32_t lane = threadIdx.x & 31u;
-  if (t >= a.n_tiles) {  // the end of the matrix closes the last row
-    if (st.open_owned && lane == 0) emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG));
-    return true;
-  }
-  const uint32_t* Ew = reinterpret_cast<const uint32_t*>(E4);  // warp's staging area
-  const Flags F = D::flags(w);
-  const int32_t total = D::run(w, qtb, lane << 1, E4 + lane);
-  const uint32_t incl = warp_incl_sum((uint32_t)total, lane);
-  const uint32_t LB = st.carryG + incl - (uint32_t)total;  // running sum before this packet
-  const uint32_t tileSum = __shfl_sync(0xFFFFFFFFu, incl, 31);
-  const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
-  if (t >= te) {  // closing: only the first flag from here on matters
-    if (has_mask == 0) {
-      st.carryG += tileSum;
-      return false;
-    }
-    if (lane == (uint32_t)(__ffs(has_mask) - 1)) {
-      const uint32_t Gb = LB + D::prefix(Ew, lane, ffs_flags(F));
-      if (st.open_owned) emit(rowbase, (int32_t)(Gb - st.startG));
-    }
-    return true;
-  }
-  const uint32_t nf = popc_flags(F);
-  const uint32_t rbase = rowbase + warp_incl_sum(nf, lane) - nf;
-  uint32_t lastGb = 0;
-  if (F) lastGb = LB + D::prefix(Ew, lane, fls_flags(F));
-  const uint32_t left = has_mask & ((1u << lane) - 1u);
-  const uint32_t inhG = __shfl_sync(0xFFFFFFFFu, lastGb, left ? (31 - __clz(left)) : 0u);
-  uint32_t prevG = left ? inhG : st.startG;
-  Flags f = F;
-  uint32_t row = rbase;
-  if (f && !left && !st.open_owned) {  // first flag closes a row started before the range
-    prevG = LB + D::prefix(Ew, lane, ffs_flags(f));
-    f &= f - 1;
-    row++;
-  }
-  if (emit.int_filter()) {
-    // the common case, chosen once outside the per-lane loop: a compare per row, and the
-    // survivor append only on a hit
-    const int32_t ts = emit.thr_score();
-    while (f) {  // each flag closes the row before it
-      const int j = ffs_flags(f);
-      f &= f - 1;
-      const uint32_t Gb = LB + D::prefix(Ew, lane, j);
-      const int32_t sc = (int32_t)(Gb - prevG);
-      if (sc >= ts) emit.append_int(row, sc);
-      prevG = Gb;
-      row++;
-    }
-  } else {
-    while (f) {  // each flag closes the row before it
-      const int j = ffs_flags(f);
-      f &= f - 1;
-      const uint32_t Gb = LB + D::prefix(Ew, lane, j);
-      emit(row, (int32_t)(Gb - prevG));
-      prevG = Gb;
-      row++;
-    }
-  }
-  if (has_mask) {
-    st.startG = __shfl_sync(0xFFFFFFFFu, lastGb, 31 - __clz(has_mask));
-    st.open_owned = true;
-  }
-  st.carryG += tileSum;
-  return false;
-}
-
 // How a plain pass emits rows: any emitter, or the filter with integer keys (no row scales) and
 // one partition, or with several partitions.
 enum EmitKind : int { EMIT_ANY = 0, EMIT_INT_ONE = 1, EMIT_INT_PARTS = 2 };
@@ -484,17 +394,18 @@ struct PartTrack {
   int32_t ts;    // score bound of partition p
 };
 
-// One tile of a warp's range (B = 8).  Returns true once the range is complete.
+// One tile of a warp's range.  Returns true once the range is complete.
 // KIND EMIT_INT_*: a compare per row against the score bound of the partition of the tile's rows
 // (the lowest over its partitions when it straddles some), and the exact check and survivor
 // append only on a hit.  CLOSING: a tile at or past the range's end, where only the first flag
 // matters.
-template <bool SGN, int MODE, int KIND, bool CLOSING>
-__device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
+template <int B, bool SGN, int MODE, int KIND, bool CLOSING>
+__device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t,
                                            const uint32_t (&w)[16], uint32_t rowbase,
                                            RangeState& st, const Emitter<MODE>& emit,
                                            const char* qtb, PartTrack& pt) {
-  using D = Packet8<SGN>;
+  using D = PacketSpans<B, SGN>;
+  using Flags = typename D::Flags;
   const uint32_t lane = threadIdx.x & 31u;
   if constexpr (CLOSING) {
     if (t >= a.n_tiles) {  // the end of the matrix closes the last row
@@ -502,12 +413,12 @@ __device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
       return true;
     }
   }
-  const uint32_t F = w[0] & ((1u << D::P) - 1u);
+  const Flags F = PacketDecoder<B, SGN>::flags(w);
   const uint32_t has_mask = __ballot_sync(0xFFFFFFFFu, F != 0);
   uint32_t rbase = rowbase;  // row closed by this lane's first flag
   int32_t ts = 0;            // EMIT_INT_*: score bound of the rows this tile closes
   if constexpr (!CLOSING) {
-    const uint32_t nf = __popc(F);
+    const uint32_t nf = popc_flags(F);
     const uint32_t incl = warp_incl_sum(nf, lane);
     rbase += incl - nf;
     if constexpr (KIND == EMIT_INT_ONE) ts = emit.thr_score();
@@ -570,7 +481,7 @@ __device__ __forceinline__ bool tile_step8(const PlainArgs& a, uint32_t t,
 // row runs on through the closing tile.
 template <int B, bool SGN, int MODE, int KIND>
 __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
-                           const Emitter<MODE>& emit, const char* qtb, uint4* E4, uint4* stg) {
+                           const Emitter<MODE>& emit, const char* qtb, uint4* stg) {
   const uint32_t lane = threadIdx.x & 31u;
   if (tb >= te) return;
   RangeState st{tb == 0, 0u, 0u};  // row 0 starts at entry 0 without a flag
@@ -609,66 +520,48 @@ __device__ void cand_range(const PlainArgs& a, uint32_t tb, uint32_t te,
     }
     const uint32_t r = rn;
     if (t + 1 <= te) fetch(t + 1);
-    if constexpr (B == 8) {
-      if (t < te) {  // te <= n_tiles
-        tile_step8<SGN, MODE, KIND, false>(a, t, w, r, st, emit, qtb, pt);
-      } else if (tile_step8<SGN, MODE, KIND, true>(a, t, w, r, st, emit, qtb, pt)) {
-        return;
-      }
-    } else {
-      if (tile_step<B, SGN, MODE>(a, t, te, w, r, st, emit, qtb, E4)) return;
+    if (t < te) {  // te <= n_tiles
+      tile_step<B, SGN, MODE, KIND, false>(a, t, w, r, st, emit, qtb, pt);
+    } else if (tile_step<B, SGN, MODE, KIND, true>(a, t, w, r, st, emit, qtb, pt)) {
+      return;
     }
     if (t + 1 > te) fetch(t + 1);
   }
 }
 
-// per warp: B = 4, 6 stage the running sum of every entry (B = 8 stages nothing)
-__host__ __device__ constexpr size_t plain_stage_bytes_of(int B) {
-  return B == 8 ? 0 : (size_t)((packet_elems(B) + 3) / 4) * 32 * 16;
-}
-// query table bytes per column: 32 lane copies, 32-bit for B = 8 (one wavefront per gather),
-// 16-bit for B = 4, 6 (lanes 2m and 2m+1 share bank m + 16 * (col & 1): at most two)
-__host__ __device__ constexpr size_t plain_table_bytes_per_col(int B) { return B == 8 ? 128 : 64; }
+// query table bytes per column: 32 lane copies of 32 bits (one wavefront per gather)
+constexpr size_t kPlainTableBytesPerCol = 128;
 constexpr size_t kPlainTileBuf = 2048;  // per warp: the next 32-packet tile
 
-// dynamic shared memory of the plain pass: lane-replicated query table, per-warp prefix
-// staging and next-tile buffer, thresholds of up to kThrSmemMax partitions
+// dynamic shared memory of the plain pass: lane-replicated query table, per-warp next-tile
+// buffer, thresholds of up to kThrSmemMax partitions
 __host__ inline size_t plain_smem_bytes(int B, uint32_t cols, uint32_t split) {
-  return (size_t)cols * plain_table_bytes_per_col(B) +
-         (size_t)plain_warps(B) * (plain_stage_bytes_of(B) + kPlainTileBuf) +
+  return (size_t)cols * kPlainTableBytesPerCol + (size_t)plain_warps(B) * kPlainTileBuf +
          (split > 1 && split <= kThrSmemMax ? split * 4ull : 0ull);
 }
 
 template <int B, bool SGN, int MODE>
 __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a) {
   constexpr int W = plain_warps(B);
-  constexpr size_t TB = plain_table_bytes_per_col(B), SB = plain_stage_bytes_of(B);
   extern __shared__ __align__(16) unsigned char smem[];
   // the warp index through a shuffle from lane 0, so the range bounds and every branch on them
   // are known to be warp-uniform
   const uint32_t warp = __shfl_sync(0xFFFFFFFFu, threadIdx.x >> 5, 0);
   const char* qtb = reinterpret_cast<const char*>(smem);  // qt[cols][32 lanes]
-  unsigned char* after = smem + (size_t)a.cols * TB;
-  uint4* E4 = reinterpret_cast<uint4*>(after) + (size_t)warp * (SB / 16);
-  uint4* stg = reinterpret_cast<uint4*>(after + W * SB) + (size_t)warp * (kPlainTileBuf / 16);
-  uint32_t* thr_s = reinterpret_cast<uint32_t*>(after + W * (SB + kPlainTileBuf));
+  unsigned char* after = smem + (size_t)a.cols * kPlainTableBytesPerCol;
+  uint4* stg = reinterpret_cast<uint4*>(after) + (size_t)warp * (kPlainTileBuf / 16);
+  uint32_t* thr_s = reinterpret_cast<uint32_t*>(after + W * kPlainTileBuf);
   // replicate the query once per lane; the bytes are staged through the (not yet used) area
   // after the table so the fill needs one global round trip
   int8_t* qstage = reinterpret_cast<int8_t*>(after);
   const int8_t* q8 = a.q8 + (size_t)blockIdx.y * a.q8_ld;
   for (uint32_t i = threadIdx.x; i < a.cols; i += blockDim.x) qstage[i] = q8[i];
   __syncthreads();
-  if constexpr (B == 8) {
+  {
     uint4* qt = reinterpret_cast<uint4*>(smem);  // four lane copies per store
     for (uint32_t i = threadIdx.x; i < a.cols * 8u; i += blockDim.x) {
       const uint32_t v = (uint8_t)qstage[i >> 3];  // the byte dp4a reads (signed or not)
       qt[i] = make_uint4(v, v, v, v);
-    }
-  } else {
-    int16_t* qt = reinterpret_cast<int16_t*>(smem);
-    for (uint32_t i = threadIdx.x; i < a.cols * 32u; i += blockDim.x) {
-      const uint32_t c = i >> 5;
-      qt[i] = SGN ? (int16_t)qstage[c] : (int16_t)(uint8_t)qstage[c];
     }
   }
   __syncthreads();
@@ -686,20 +579,20 @@ __global__ void __launch_bounds__(plain_threads(B), 1) k_cand_plain(PlainArgs a)
       const uint32_t t = s * a.sample_stride;
       // keys of query y land keys_ld further on: the index row - base wraps to that offset
       Emitter<MODE> em{a, thr_s, thr0, __ldg(a.sample_first + s) - blockIdx.y * a.keys_ld};
-      cand_range<B, SGN, MODE, EMIT_ANY>(a, t, t + 1, em, qtb, E4, stg);
+      cand_range<B, SGN, MODE, EMIT_ANY>(a, t, t + 1, em, qtb, stg);
     }
   } else {
     const uint64_t n = a.n_tiles;
     const uint32_t tb = (uint32_t)((n * gw) / nw), te = (uint32_t)((n * (gw + 1)) / nw);
     Emitter<MODE> em{a, thr_s, thr0, 0u};
-    if constexpr (B == 8 && MODE == MODE_FILTER) {
+    if constexpr (MODE == MODE_FILTER) {
       if (em.int_keys()) {
-        if (a.split <= 1) cand_range<B, SGN, MODE, EMIT_INT_ONE>(a, tb, te, em, qtb, E4, stg);
-        else cand_range<B, SGN, MODE, EMIT_INT_PARTS>(a, tb, te, em, qtb, E4, stg);
+        if (a.split <= 1) cand_range<B, SGN, MODE, EMIT_INT_ONE>(a, tb, te, em, qtb, stg);
+        else cand_range<B, SGN, MODE, EMIT_INT_PARTS>(a, tb, te, em, qtb, stg);
         return;
       }
     }
-    cand_range<B, SGN, MODE, EMIT_ANY>(a, tb, te, em, qtb, E4, stg);
+    cand_range<B, SGN, MODE, EMIT_ANY>(a, tb, te, em, qtb, stg);
   }
 }
 
