@@ -426,6 +426,27 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
   }
 }
 
+// Sample keys of one batched block, [rows][128 queries] as the batched sample pass writes them,
+// to [query][rows] (the plain layout), so the threshold pass reads each query's keys
+// contiguously instead of one 32-byte sector per key.  A CTA moves 32 rows x 128 queries through
+// shared memory; both the reads and the writes are coalesced.
+constexpr uint32_t kTransposeRows = 32;
+__global__ void __launch_bounds__(256) k_keys_transpose(const uint32_t* __restrict__ in,
+                                                        uint32_t n_rows, uint32_t nq,
+                                                        uint32_t* __restrict__ out) {
+  __shared__ uint32_t t[kTransposeRows][kBatchQ + 1];
+  const uint32_t r0 = blockIdx.x * kTransposeRows;
+  for (uint32_t i = threadIdx.x; i < kTransposeRows * kBatchQ; i += blockDim.x) {
+    const uint32_t rr = i / kBatchQ, q = i % kBatchQ;
+    if (r0 + rr < n_rows) t[rr][q] = in[(size_t)(r0 + rr) * kBatchQ + q];
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < kTransposeRows * kBatchQ; i += blockDim.x) {
+    const uint32_t q = i / kTransposeRows, rr = i % kTransposeRows;
+    if (q < nq && r0 + rr < n_rows) out[(size_t)q * n_rows + r0 + rr] = t[rr][q];
+  }
+}
+
 // qtab[col][33] words: byte t of word (col, l) = quantised query q0 + 4l + t at col (0 past nq);
 // word 32 of each column and the padding to a 16-byte slot are zero
 __global__ void k_qtable(const int8_t* __restrict__ q8, uint32_t ld8, uint32_t cols, uint32_t q0,

@@ -128,6 +128,7 @@ struct Engine {
   float* d_q32 = nullptr;
   int8_t* d_q8 = nullptr;
   uint32_t* d_sample_keys = nullptr;
+  uint32_t* d_keys_t = nullptr;   // batched sample keys moved to [query][sample rows]
   uint32_t* d_thr = nullptr;
   uint32_t* d_cnt = nullptr;
   uint2* d_surv = nullptr;
@@ -203,7 +204,7 @@ struct Engine {
     d_sample_first = d_part_sample_begin = d_part_r = nullptr;
     d_q32 = nullptr;
     d_q8 = nullptr;
-    d_sample_keys = d_thr = d_cnt = d_cand = d_cand_key = d_status = d_out_idx = nullptr;
+    d_sample_keys = d_keys_t = d_thr = d_cnt = d_cand = d_cand_key = d_status = d_out_idx = nullptr;
     d_surv = nullptr;
     d_out_score = nullptr;
     d_exact_cand = d_exact_key = d_qtab = nullptr;
@@ -362,6 +363,7 @@ int Engine::plan_config(const aes_params& p, Config* c) const {
   const size_t nblk = (maxB + kBatchQ - 1) / kBatchQ;
   size_t plan = (c->n_sample_tiles + 2ull * S + 2) * 4;
   plan += nblk * kBatchQ * (size_t)c->n_sample_rows * 4;
+  plan += maxB * (size_t)c->n_sample_rows * 4;  // the same keys, query-major
   plan += maxB * (ld32 * 4ull + ld8 + S * 8ull + (size_t)S * c->cap * 8 + c->nslots * 8ull + 4 +
                   p.k_max * 8ull);
   plan += nblk * batch_qtab_words(cols) * 4;
@@ -398,6 +400,7 @@ int Engine::apply_config(const Config& c) {
   // batched passes write sample keys per block of kBatchQ queries: pad to whole blocks
   const size_t maxB_blk = (size_t)((maxB + kBatchQ - 1) / kBatchQ) * kBatchQ;
   AES_AL(d_sample_keys, maxB_blk * std::max<uint32_t>(n_sample_rows, 1));
+  AES_AL(d_keys_t, (size_t)maxB * std::max<uint32_t>(n_sample_rows, 1));
   AES_AL(d_thr, (size_t)maxB * split);
   AES_AL(d_cnt, (size_t)maxB * split);
   AES_AL(d_surv, (size_t)maxB * split * cap);
@@ -718,7 +721,17 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
       if (rc) return rc;
     }
   }
-  k_threshold<<<dim3(split, nq), kThreadsThr, 0, s>>>(d_sample_keys, n_sample_rows, batched ? kBatchQ : 0,
+  if (batched && n_sample_rows) {  // the threshold pass reads each query's keys contiguously
+    for (uint32_t b = 0; b < nblk; b++) {
+      const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
+      const size_t off = (size_t)b * kBatchQ * n_sample_rows;
+      k_keys_transpose<<<(n_sample_rows + kTransposeRows - 1) / kTransposeRows, 256, 0, s>>>(
+          d_sample_keys + off, n_sample_rows, nb, d_keys_t + off);
+      AES_CK(cudaGetLastError());
+      n_launch++;
+    }
+  }
+  k_threshold<<<dim3(split, nq), kThreadsThr, 0, s>>>(batched ? d_keys_t : d_sample_keys, n_sample_rows, 0,
                                               d_part_sample_begin, split, d_part_r, d_thr, d_cnt);
   AES_CK(cudaGetLastError());
   if (batched) {
