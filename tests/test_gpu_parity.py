@@ -331,3 +331,21 @@ def test_query_quantiser_on_rounding_ties(bits, quant, qq):
             q = q * np.where(rng.random(cols) < 0.5, -1, 1).astype(np.float32)
         got = eng.score_all(q)
         assert np.array_equal(got, m.keys(q, qq=qq)), f"trial {trial}"
+
+
+@pytest.mark.parametrize("kind,rows,p0,p1,bits,quant,split", [
+    (E.GEN_UNIFORM_DEG, 400000, 10, 30, 8, 0, 1),
+    (E.GEN_UNIFORM_DEG, 400000, 10, 30, 6, 0, 32),
+    (E.GEN_UNIFORM_DEG, 400000, 10, 30, 4, 2, 1),
+    (E.GEN_GAMMA_DEG, 150000, 120, 700, 8, 1, 8),
+])
+def test_rows_across_range_boundaries_at_scale(kind, rows, p0, p1, bits, quant, split):
+    """Matrices large enough that every warp's range spans several tiles, so thousands of rows
+    cross a boundary between two warps' ranges (and long rows cross several tiles).  Every
+    row's key and the two-stage results must equal the oracle's."""
+    cols, k, ck = 1024, 100, 1024
+    m, eng = make(rows, cols, kind, p0, p1, 61, bits, quant, split, ck, k, nq=2)
+    Q = queries(cols, 2, 13, signed=(quant == 0))
+    for q in Q:
+        assert np.array_equal(eng.score_all(q), m.keys(q))
+    check_run(m, eng, Q, split, ck, k)
