@@ -160,6 +160,91 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+SMALL_METRIC = "Top-100 queries/s, 400k×500 |N(0,1)| 69 nnz/row, 6-bit, SPLIT=32, CK=512 (plain method, small)"
+
+
+def run_small(args, rank, world):
+    """The reference's small plain-method configuration: 400,000 x 500 at 69 distinct uniform
+    columns per row, FP32 values |N(0,1)|, the reference's global 6-bit quantiser, SPLIT=32,
+    CK=512, K=100; 100 queries, each a densified random row.  Plain (one candidate pass per
+    query) and batched paths on the GPU, every query checked against the oracle, and the
+    reference's CPU method on this host's cores."""
+    if rank != 0:
+        return
+    import torch
+    import oracle as orc
+    from acceles_gb300 import engine as E
+    rows, cols, nq, split, ck = 400_000, 500, 100, 32, 512
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    ptr, col, val = E.gen_matrix(E.GEN_FIXED_ABSNORMAL, rows, cols, 69, 0, seed=SEED)
+    rng = np.random.default_rng(SEED + 7)
+    Q = np.zeros((nq, cols), np.float32)
+    for i, r in enumerate(rng.integers(0, rows, nq)):
+        Q[i, col[ptr[r]:ptr[r + 1]]] = val[ptr[r]:ptr[r + 1]]
+    stream = torch.cuda.Stream()
+    dq = torch.from_numpy(Q).cuda()
+    di = torch.empty((nq, K), dtype=torch.int32, device="cuda")
+    ds = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+    out = {}
+    for name, bt in (("plain", 1), ("batched", 128)):
+        eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=6, quant=E.QUANT_SYM_GLOBAL,
+                     split=split, ck=ck, k_max=K, max_batch=nq, batch_tile=bt,
+                     flags=E.FLAG_PROFILE)
+        run = lambda: eng.run_device(dq.data_ptr(), nq, K, di.data_ptr(), ds.data_ptr(),
+                                     stream.cuda_stream)
+        for _ in range(args.warmup):
+            run()
+        torch.cuda.synchronize()
+        eng.finish()
+        eng.stats(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        st = eng.stats(reset=True)
+        info = eng.info()
+        cand_ms = st["cand_ms"] / max(st["cand_timed"], 1)
+        out[name] = {"queries_per_s": nq / (ms / 1e3), "ms_per_step": ms,
+                     "cand_pass_ms": cand_ms,
+                     "cand_pass_gbs": ((info["packets"] * 64 + (info["tiles"] + 1) * 4) / (cand_ms / 1e3) / 1e9
+                                       if cand_ms > 0 else None),
+                     "repaired": eng.finish() + st["repaired"]}
+        # every query against the oracle (outside the timed region)
+        eng.Q_reset(Q)
+        eng(k=K)
+        idx, sc = eng.read_topk()
+        m = orc.Matrix(rows, cols, ptr, col, val, 6, orc.QUANT_SYM_GLOBAL)
+        exact, rec = True, []
+        for i in range(nq):
+            oi, os_, _ = m.two_stage(Q[i], split, ck, K)
+            exact &= bool(np.array_equal(idx[i, :len(oi)], oi)) and bool(np.array_equal(sc[i, :len(oi)], os_))
+            f64 = orc.scores_f64(m.ptr, m.col, m.val, Q[i], rows)
+            top = np.argsort(-f64, kind="stable")[:K]
+            rec.append(len(set(top.tolist()) & set(idx[i].tolist())) / K)
+        out[name]["bit_exact_vs_oracle"] = exact
+        out[name]["recall_at_100_vs_fp64_min"] = min(rec)
+        eng.close()
+    threads = os.cpu_count() or 1
+    el, done, _ = orc.bench_two_stage(m, Q, ck, K, nthreads=threads, max_seconds=args.cpu_seconds)
+    el1, d1, _ = orc.bench_two_stage(m, Q, ck, K, nthreads=1, max_seconds=max(2.0, args.cpu_seconds / 3))
+    line = {"metric": SMALL_METRIC, "value": out["plain"]["queries_per_s"], "unit": "queries/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded; reference matrices not shipped)",
+            "config": {"workload": "400kx500 69 nnz/row |N(0,1)|, 6-bit symmetric Ultra-CSR, SPLIT=32, CK=512, K=100, 100 densified-row queries",
+                       "rows": rows, "cols": cols, "nnz": int(ptr[-1]), "bits": 6, "split": split,
+                       "ck": ck, "k": K, "l2": "packets (about 59 MB) fit in L2"},
+            "plain": out["plain"], "batched": out["batched"],
+            "cpu_baseline": {"value": done / el, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{done} queries: two-stage method, global Top-{ck} "
+                                       f"(gold_algorithms.hpp:249-308), FP32 rescoring, {threads} threads, {el:.1f} s",
+                             "two_stage_1_thread": d1 / el1}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -175,6 +260,8 @@ def main():
     ap.add_argument("--no-gpu-baseline", action="store_true")
     ap.add_argument("--check", type=int, default=2, help="queries checked against the oracle")
     ap.add_argument("--rows", type=int, default=ROWS, help="smaller matrix, for profiling only")
+    ap.add_argument("--workload", default="large", choices=["large", "small"],
+                    help="large: 10M x 1024 (the headline); small: the 400k x 500 plain-method case")
     ap.add_argument("--split", type=int, default=1,
                     help="row partitions with a Top-(CK/split) each (the reference default is 32)")
     args = ap.parse_args()
@@ -187,6 +274,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "small":
+        run_small(args, rank, world)
         return
 
     import torch
