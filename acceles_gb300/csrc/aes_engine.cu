@@ -129,6 +129,7 @@ struct Engine {
   int8_t* d_q8 = nullptr;
   uint32_t* d_sample_keys = nullptr;
   uint32_t* d_keys_t = nullptr;   // batched sample keys moved to [query][sample rows]
+  uint32_t* d_exact_aux = nullptr;  // FP32-only pass: sample range {0, n} and rank r
   uint32_t* d_thr = nullptr;
   uint32_t* d_cnt = nullptr;
   uint2* d_surv = nullptr;
@@ -207,7 +208,7 @@ struct Engine {
     d_sample_keys = d_keys_t = d_thr = d_cnt = d_cand = d_cand_key = d_status = d_out_idx = nullptr;
     d_surv = nullptr;
     d_out_score = nullptr;
-    d_exact_cand = d_exact_key = d_qtab = nullptr;
+    d_exact_cand = d_exact_key = d_qtab = d_exact_aux = nullptr;
     bytes -= cfg_bytes;
     cfg_bytes = 0;
     configured = false;
@@ -412,6 +413,7 @@ int Engine::apply_config(const Config& c) {
   AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * batch_qtab_words(cols));
   AES_AL(d_exact_cand, std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_exact_key, std::max<uint32_t>(p.k_max, 1));
+  AES_AL(d_exact_aux, 4);
 #undef AES_AL
   AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
   AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
@@ -1145,48 +1147,101 @@ int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score
   AES_CK(cudaSetDevice(e.device));
   uint32_t kp = 1;
   while (kp < k) kp <<= 1;
+  // Filtered select: every S-th row key is a sample; its r-th largest key lies below the K-th
+  // largest key of all rows except with probability 1e-12 (binomial tail), so only the rows at or
+  // above it need the select.  S is the largest power of two whose expected survivors fit the
+  // survivor buffer; a miss or an overflow is detected by the select and falls back to the
+  // select over every row, so the result is exact either way.
+  uint32_t S = 0, r = 0;
+  for (uint32_t cs = 1024; cs >= 2 && e.rows >= 4u * k; cs >>= 1) {
+    const uint32_t nsm = (e.rows + cs - 1) / cs;
+    const double f = 1.0 / cs;
+    const uint32_t n1 = k - 1;
+    uint32_t rr = (uint32_t)std::floor(n1 * f);
+    while (rr <= n1 && aes::binom_tail(n1, f, rr) > 1e-12) rr++;
+    rr = std::max<uint32_t>(rr, 1);
+    if (rr > nsm) continue;
+    if (2.0 * rr / f + k + 64.0 <= (double)e.cap) {
+      S = cs;
+      r = rr;
+      break;
+    }
+  }
+  if (S) {
+    const uint32_t aux[3] = {0u, (e.rows + S - 1) / S, r};
+    AES_CK(cudaMemcpy(e.d_exact_aux, aux, sizeof(aux), cudaMemcpyHostToDevice));
+  }
+  FinalArgs fa{};
+  fa.csr_ptr = e.d_csr_ptr;
+  fa.csr_col = e.d_csr_col;
+  fa.csr_val = e.d_csr_val;
+  fa.ld32 = e.ld32;
+  fa.cols = e.cols;
+  fa.cand = e.d_exact_cand;
+  fa.nslots = k;
+  fa.kp = kp;
+  fa.k = k;
+  fa.out_idx = e.d_out_idx;
+  fa.out_score = e.d_out_score;
+  fa.status = nullptr;
+  SelectArgs sa{};
+  sa.q0 = 0;
+  sa.split = 1;
+  sa.slice = e.rows;
+  sa.n_rows = e.rows;
+  sa.ntop = k;
+  sa.cand = e.d_exact_cand;
+  sa.cand_key = e.d_exact_key;
+  sa.status = e.d_status;
   float total_ms = 0.0f;
   for (uint32_t q = 0; q < e.nq_loaded; q++) {
+    fa.q32 = e.d_q32 + (size_t)q * e.ld32;
+    AES_CK(cudaMemsetAsync(e.d_status, 0, 4, e.stream));
     AES_CK(cudaEventRecord(e.ev0, e.stream));
-    k_exact_all<<<e.sm_count * 8, 256, e.cols * 4, e.stream>>>(
+    k_exact_all<<<e.sm_count * 8, kExactWarps * 32, exact_all_smem_bytes(e.cols), e.stream>>>(
         e.d_csr_ptr, e.d_csr_col, e.d_csr_val, e.d_q32 + (size_t)q * e.ld32, e.cols, e.rows,
         e.d_allkeys);
     AES_CK(cudaGetLastError());
-    SelectArgs sa{};
-    sa.allkeys = e.d_allkeys;
-    sa.q0 = 0;
-    sa.split = 1;
-    sa.slice = e.rows;
-    sa.n_rows = e.rows;
-    sa.ntop = k;
-    sa.cand = e.d_exact_cand;
-    sa.cand_key = e.d_exact_key;
-    sa.status = e.d_status;
-    k_select<true><<<dim3(1, 1), 512, 0, e.stream>>>(sa);
+    if (S) {
+      k_threshold<<<dim3(1, 1), kThreadsThr, 0, e.stream>>>(e.d_allkeys, 0, S, e.d_exact_aux, 1,
+                                                           e.d_exact_aux + 2, e.d_thr, e.d_cnt);
+      AES_CK(cudaGetLastError());
+      k_filter_keys<<<e.sm_count * 4, 256, 0, e.stream>>>(e.d_allkeys, e.rows, e.d_thr, e.d_cnt,
+                                                         e.d_surv, e.cap);
+      AES_CK(cudaGetLastError());
+      sa.surv = e.d_surv;
+      sa.cnt = e.d_cnt;
+      sa.cap = e.cap;
+      k_select<false><<<dim3(1, 1), 512, 0, e.stream>>>(sa);
+    } else {
+      sa.allkeys = e.d_allkeys;
+      k_select<true><<<dim3(1, 1), 512, 0, e.stream>>>(sa);
+    }
     AES_CK(cudaGetLastError());
-    FinalArgs fa{};
-    fa.csr_ptr = e.d_csr_ptr;
-    fa.csr_col = e.d_csr_col;
-    fa.csr_val = e.d_csr_val;
-    fa.q32 = e.d_q32 + (size_t)q * e.ld32;
-    fa.ld32 = e.ld32;
-    fa.cols = e.cols;
-    fa.cand = e.d_exact_cand;
-    fa.nslots = k;
-    fa.kp = kp;
-    fa.k = k;
-    fa.out_idx = e.d_out_idx;
-    fa.out_score = e.d_out_score;
-    fa.status = nullptr;
     k_final<<<1, kThreadsFinal, e.final_smem, e.stream>>>(fa);
     AES_CK(cudaGetLastError());
     AES_CK(cudaEventRecord(e.ev1, e.stream));
-    AES_CK(cudaMemcpyAsync(out_idx + (size_t)q * k, e.d_out_idx, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
-    AES_CK(cudaMemcpyAsync(out_score + (size_t)q * k, e.d_out_score, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
+    AES_CK(cudaMemcpyAsync(e.h_status, e.d_status, 4, cudaMemcpyDeviceToHost, e.stream));
     AES_CK(cudaStreamSynchronize(e.stream));
     float ms = 0.0f;
     AES_CK(cudaEventElapsedTime(&ms, e.ev0, e.ev1));
     total_ms += ms;
+    if (S && e.h_status[0]) {  // the sample bound missed or the buffer overflowed: every row
+      AES_CK(cudaEventRecord(e.ev0, e.stream));
+      sa.allkeys = e.d_allkeys;
+      k_select<true><<<dim3(1, 1), 512, 0, e.stream>>>(sa);
+      AES_CK(cudaGetLastError());
+      k_final<<<1, kThreadsFinal, e.final_smem, e.stream>>>(fa);
+      AES_CK(cudaGetLastError());
+      AES_CK(cudaEventRecord(e.ev1, e.stream));
+      AES_CK(cudaStreamSynchronize(e.stream));
+      AES_CK(cudaEventElapsedTime(&ms, e.ev0, e.ev1));
+      total_ms += ms;
+      e.n_repaired++;
+    }
+    AES_CK(cudaMemcpyAsync(out_idx + (size_t)q * k, e.d_out_idx, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
+    AES_CK(cudaMemcpyAsync(out_score + (size_t)q * k, e.d_out_score, k * 4ull, cudaMemcpyDeviceToHost, e.stream));
+    AES_CK(cudaStreamSynchronize(e.stream));
   }
   if (ns) *ns = (uint64_t)((double)total_ms * 1e6);
   return AES_OK;

@@ -1120,29 +1120,76 @@ __global__ void __launch_bounds__(kThreadsFinal, 2) k_final(FinalArgs a) {
 namespace aes {
 namespace dev {
 
-// FP32 score of every row (sequential over the row's entries in column order, separately
-// rounded multiply and add: spmv_coo_gold_top_k, gold_algorithms.hpp:189-247 with V = float)
-// written as order-preserving keys.  Thread per row; the query is staged in shared memory.
-__global__ void k_exact_all(const uint32_t* __restrict__ ptr, const uint16_t* __restrict__ col,
-                            const float* __restrict__ val, const float* __restrict__ q,
-                            uint32_t cols, uint32_t rows, uint32_t* __restrict__ keys) {
-  extern __shared__ float qs[];
+// FP32-only pass: the FP32 score of every row (each row summed in column order with separately
+// rounded multiply and add: spmv_coo_gold_top_k, gold_algorithms.hpp:189-247 with V = float) as an
+// order-preserving key.
+// A warp takes 32 consecutive rows, one per lane.  Their entries are contiguous in the CSR, so
+// the warp stages them through shared memory in chunks of kExactChunk with coalesced loads, and
+// each lane then sums its own row's part of each chunk.
+constexpr uint32_t kExactChunk = 512;       // entries per warp and chunk
+constexpr uint32_t kExactWarps = 8;         // warps per CTA
+__host__ inline size_t exact_all_smem_bytes(uint32_t cols) {
+  return (size_t)cols * 4 + (size_t)kExactWarps * kExactChunk * 6;
+}
+
+__global__ void __launch_bounds__(kExactWarps * 32) k_exact_all(
+    const uint32_t* __restrict__ ptr, const uint16_t* __restrict__ col,
+    const float* __restrict__ val, const float* __restrict__ q, uint32_t cols, uint32_t rows,
+    uint32_t* __restrict__ keys) {
+  extern __shared__ __align__(16) unsigned char xsm[];
+  float* qs = reinterpret_cast<float*>(xsm);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  float* sv = reinterpret_cast<float*>(xsm + (size_t)cols * 4) + warp * kExactChunk;
+  uint16_t* sc = reinterpret_cast<uint16_t*>(xsm + (size_t)cols * 4 + kExactWarps * kExactChunk * 4) +
+                 warp * kExactChunk;
   for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) qs[j] = q[j];
   __syncthreads();
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-    uint32_t e = ptr[r];
-    const uint32_t e1 = ptr[r + 1];
+  const uint32_t nblk = (rows + 31) / 32;
+  for (uint32_t blk = blockIdx.x * kExactWarps + warp; blk < nblk; blk += gridDim.x * kExactWarps) {
+    const uint32_t r0 = blk * 32, r = r0 + lane;
+    const uint32_t rend = min(r0 + 32u, rows);
+    const uint32_t E0 = ptr[r0], E1 = ptr[rend];
+    const uint32_t s = r < rows ? ptr[r] : E1, e = r < rows ? ptr[r + 1] : E1;
     float acc = 0.0f;
-    for (; e + 4 <= e1; e += 4) {
-      const uint16_t c0 = col[e], c1 = col[e + 1], c2 = col[e + 2], c3 = col[e + 3];
-      const float v0 = val[e], v1 = val[e + 1], v2 = val[e + 2], v3 = val[e + 3];
-      acc = __fadd_rn(acc, __fmul_rn(v0, qs[c0]));
-      acc = __fadd_rn(acc, __fmul_rn(v1, qs[c1]));
-      acc = __fadd_rn(acc, __fmul_rn(v2, qs[c2]));
-      acc = __fadd_rn(acc, __fmul_rn(v3, qs[c3]));
+    for (uint32_t c = E0; c < E1; c += kExactChunk) {
+      const uint32_t n = min(kExactChunk, E1 - c);
+#pragma unroll 4
+      for (uint32_t i = lane; i < n; i += 32) {
+        sv[i] = val[c + i];
+        sc[i] = col[c + i];
+      }
+      __syncwarp();
+      const uint32_t a = max(s, c), b = min(e, c + n);
+      for (uint32_t i = a; i < b; i++) acc = __fadd_rn(acc, __fmul_rn(sv[i - c], qs[sc[i - c]]));
+      __syncwarp();
     }
-    for (; e < e1; e++) acc = __fadd_rn(acc, __fmul_rn(val[e], qs[col[e]]));
-    keys[r] = key_f32(acc);
+    if (r < rows) keys[r] = key_f32(acc);
+  }
+}
+
+// Rows whose key is at least *thr, appended as (key, row) to surv (warp-aggregated counter; the
+// count goes on past cap so the select can tell an overflow).  Used by the FP32-only pass after
+// a sample threshold, so that the select reads a few survivors instead of every row.
+__global__ void k_filter_keys(const uint32_t* __restrict__ keys, uint32_t rows,
+                              const uint32_t* __restrict__ thr, uint32_t* __restrict__ cnt,
+                              uint2* __restrict__ surv, uint32_t cap) {
+  const uint32_t th = *thr, lane = threadIdx.x & 31u;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t n_iter = (rows + stride - 1) / stride;  // the same for every lane of a warp
+  for (uint32_t it = 0; it < n_iter; it++) {
+    const uint32_t r = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t key = r < rows ? keys[r] : 0u;
+    const bool hit = r < rows && key >= th;
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
+    if (m) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(cnt, (uint32_t)__popc(m));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (hit) {
+        const uint32_t i = base + __popc(m & ((1u << lane) - 1u));
+        if (i < cap) surv[i] = make_uint2(key, r);
+      }
+    }
   }
 }
 

@@ -271,18 +271,38 @@ def test_batched_tiny_and_zero_queries():
     check_run(m, eng, Q, 32, 64, 10)
 
 
-def test_fp32_only_exact_path():
-    """aes_run_exact: FP32 score of every row + Top-K equals the FP32 oracle (sw_test path)."""
+@pytest.mark.parametrize("case", ["uniform", "even_rows_low", "large_k", "absnormal"])
+def test_fp32_only_exact_path(case):
+    """aes_run_exact: FP32 score of every row + Top-K equals the FP32 oracle (sw_test path).
+    The select reads only the rows above a bound taken from every S-th row's key; in
+    "even_rows_low" every sampled row scores low, the bound admits too many rows, and the call
+    falls back to the select over every row (counted as repaired); "large_k" has no room for a
+    sample bound and selects over every row directly."""
     rows, cols, k = 30000, 1024, 100
-    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 51, 8, 0, 1, 256, k, nq=2)
-    Q = queries(cols, 2, 52, signed=True)
+    kind, p0, p1 = E.GEN_UNIFORM_DEG, 10, 30
+    if case == "large_k":
+        k = 1000
+    if case == "absnormal":
+        rows, cols, kind, p0, p1 = 40000, 500, E.GEN_FIXED_ABSNORMAL, 69, 0
+    ptr, col, val = E.gen_matrix(kind, rows, cols, p0, p1, seed=51)
+    if case == "even_rows_low":
+        val = val.copy()
+        even = np.repeat(np.arange(rows) % 2 == 0, np.diff(ptr).astype(np.int64))
+        val[even] *= np.float32(1e-3)
+    m = orc.Matrix(rows, cols, ptr, col, val, 8, 0)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=8, quant=0, split=1, ck=256,
+                 k_max=k, max_batch=2)
+    Q = queries(cols, 2, 52, signed=(case != "even_rows_low"))
     eng.Q_reset(Q)
+    eng.stats(reset=True)
     idx, sc, ns = eng.run_exact(k=k)
     allrows = np.arange(rows, dtype=np.uint32)
     for i in range(2):
         s = orc.rescore_f32(m.ptr, m.col, m.val, Q[i], allrows)
         ri, rs = orc.sort_tuples_f32(allrows, s)
         assert np.array_equal(idx[i], ri[:k]) and np.array_equal(sc[i], rs[:k])
+    if case == "even_rows_low":
+        assert eng.stats(reset=True)["repaired"] >= 1
 
 
 @pytest.mark.parametrize("bits,quant,split,ck,k,nq", [(8, 0, 1, 4096, 1024, 3), (8, 1, 32, 2048, 1000, 20),
