@@ -389,6 +389,16 @@ def main():
         except Exception as ex:  # report, do not fail the bench
             gpu_lib = {"unavailable": str(ex)[:200]}
 
+    # the FP32-only exact Top-K of the same engine (aes_run_exact: FP32 score of every row, then
+    # the Top-K), device time per query; the reference's FP32 method on the GPU
+    exact = None
+    if rank == 0:
+        eng.Q_reset(Qh[:16])
+        ei, es, ens = eng.run_exact(k=K)
+        exact = {"method": "FP32 score of every row (column-order sums) + Top-K select",
+                 "ms_per_query": ens / 1e6 / 16, "queries_per_s": 16 / (ens / 1e9),
+                 "queries_timed": 16}
+
     # correctness of the measured configuration (outside the timed regions)
     line_extra = {}
     if rank == 0:
@@ -401,14 +411,20 @@ def main():
         eng.Q_reset(Qh[:B])
         eng(k=K)
         ri, rs = eng.read_topk()
-        recalls, exact = [], True
+        recalls, exact_ok = [], True
         for i in range(min(args.check, B)):
             oi, os_, _ = m.two_stage(Qh[i], args.split, CK, K)
-            exact &= bool(np.array_equal(ri[i], oi)) and bool(np.array_equal(rs[i], os_))
+            exact_ok &= bool(np.array_equal(ri[i], oi)) and bool(np.array_equal(rs[i], os_))
             f64 = orc.scores_f64(m.ptr, m.col, m.val, Qh[i], rows)
             top = np.argsort(-f64, kind="stable")[:K]
             recalls.append(len(set(top.tolist()) & set(ri[i].tolist())) / K)
-        line_extra = {"parity_checked_queries": min(args.check, B), "bit_exact_vs_oracle": exact,
+        if exact is not None and args.check > 0:
+            allrows = np.arange(rows, dtype=np.uint32)
+            s0 = orc.rescore_f32(m.ptr, m.col, m.val, Qh[0], allrows)
+            xi, xs = orc.sort_tuples_f32(allrows, s0)
+            exact["bit_exact_vs_oracle"] = bool(np.array_equal(ei[0], xi[:K])) and \
+                bool(np.array_equal(es[0], xs[:K]))
+        line_extra = {"parity_checked_queries": min(args.check, B), "bit_exact_vs_oracle": exact_ok,
                       "recall_at_100_vs_fp64": min(recalls) if recalls else None}
         if cb:
             line_extra["cpu_baseline"] = cb
@@ -444,6 +460,7 @@ def main():
             "gpu_launches": st["launches"], "repaired_queries": repaired + st["repaired"] + rep_p + st_p["repaired"],
             "clocks": clk, "clocks_plain": clk_p,
             "gpu_library_baseline": gpu_lib,
+            "gpu_fp32_exact": exact,
         }
         line.update(line_extra)
         print(json.dumps(line), flush=True)
