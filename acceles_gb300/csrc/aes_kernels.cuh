@@ -669,8 +669,8 @@ __global__ void k_quantize(const float* __restrict__ q32, uint32_t cols, uint32_
 // block helpers
 // ---------------------------------------------------------------------------------------------
 constexpr int kHistBins = 2048;
-constexpr int kThrILP = 8;  // keys in flight per thread in the threshold passes
-constexpr int kThreadsThr = 256;  // 80 registers: three CTAs per SM, a 256-query batch in one wave
+constexpr int kThrILP = 4;  // keys in flight per thread in the threshold passes
+constexpr int kThreadsThr = 512;  // at most 64 registers: two CTAs per SM, a 256-query batch in one wave
 
 // Largest bin b with sum(hist[b..]) >= need; *above = sum(hist[b+1..]).  Executed by warp 0.
 __device__ __forceinline__ void warp_find_suffix_bin(const uint32_t* hist, int nbins,
@@ -719,7 +719,7 @@ __device__ __forceinline__ void warp_find_suffix_bin(const uint32_t* hist, int n
 // Sample keys of query q: keys[base(q) + i * stride] with base(q) = q * ld_keys and stride 1
 // (one query per pass), or, when qblk > 0 (batched passes of qblk queries),
 // base(q) = (q / qblk) * qblk * ld_keys + q % qblk and stride qblk.
-__global__ void k_threshold(const uint32_t* __restrict__ keys_all, uint32_t ld_keys, uint32_t qblk,
+__global__ void __launch_bounds__(kThreadsThr, 2) k_threshold(const uint32_t* __restrict__ keys_all, uint32_t ld_keys, uint32_t qblk,
                             const uint32_t* __restrict__ part_begin, uint32_t split,
                             const uint32_t* __restrict__ r_part, uint32_t* __restrict__ thr,
                             uint32_t* __restrict__ cnt) {
