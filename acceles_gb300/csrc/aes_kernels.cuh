@@ -1122,14 +1122,15 @@ namespace dev {
 
 // FP32-only pass: the FP32 score of every row (each row summed in column order with separately
 // rounded multiply and add: spmv_coo_gold_top_k, gold_algorithms.hpp:189-247 with V = float) as an
-// order-preserving key.
-// A warp takes 32 consecutive rows, one per lane.  Their entries are contiguous in the CSR, so
-// the warp stages them through shared memory in chunks of kExactChunk with coalesced loads, and
-// each lane then sums its own row's part of each chunk.
+// order-preserving key.  A warp takes 32 consecutive rows, one per lane.  Their entries are
+// contiguous in the CSR, so the warp walks them in chunks of kExactChunk: every lane loads entries
+// of the chunk (coalesced, all loads in flight at once) and stores their rounded products
+// v * q[col] to shared memory in entry order; then each lane adds its own row's products of the
+// chunk in order.  The products and the order of the additions are those of the sequential sum.
 constexpr uint32_t kExactChunk = 512;       // entries per warp and chunk
 constexpr uint32_t kExactWarps = 8;         // warps per CTA
 __host__ inline size_t exact_all_smem_bytes(uint32_t cols) {
-  return (size_t)cols * 4 + (size_t)kExactWarps * kExactChunk * 6;
+  return (size_t)cols * 4 + (size_t)kExactWarps * kExactChunk * 4;
 }
 
 __global__ void __launch_bounds__(kExactWarps * 32) k_exact_all(
@@ -1139,9 +1140,7 @@ __global__ void __launch_bounds__(kExactWarps * 32) k_exact_all(
   extern __shared__ __align__(16) unsigned char xsm[];
   float* qs = reinterpret_cast<float*>(xsm);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  float* sv = reinterpret_cast<float*>(xsm + (size_t)cols * 4) + warp * kExactChunk;
-  uint16_t* sc = reinterpret_cast<uint16_t*>(xsm + (size_t)cols * 4 + kExactWarps * kExactChunk * 4) +
-                 warp * kExactChunk;
+  float* sp = reinterpret_cast<float*>(xsm + (size_t)cols * 4) + warp * kExactChunk;
   for (uint32_t j = threadIdx.x; j < cols; j += blockDim.x) qs[j] = q[j];
   __syncthreads();
   const uint32_t nblk = (rows + 31) / 32;
@@ -1153,14 +1152,19 @@ __global__ void __launch_bounds__(kExactWarps * 32) k_exact_all(
     float acc = 0.0f;
     for (uint32_t c = E0; c < E1; c += kExactChunk) {
       const uint32_t n = min(kExactChunk, E1 - c);
-#pragma unroll 4
-      for (uint32_t i = lane; i < n; i += 32) {
-        sv[i] = val[c + i];
-        sc[i] = col[c + i];
+      float lv[kExactChunk / 32];
+      uint32_t lc[kExactChunk / 32];
+#pragma unroll
+      for (uint32_t u = 0; u < kExactChunk / 32; u++) {
+        const uint32_t i = u * 32 + lane;
+        lv[u] = i < n ? __ldcs(val + c + i) : 0.0f;
+        lc[u] = i < n ? (uint32_t)__ldcs(col + c + i) : 0u;
       }
+#pragma unroll
+      for (uint32_t u = 0; u < kExactChunk / 32; u++) sp[u * 32 + lane] = __fmul_rn(lv[u], qs[lc[u]]);
       __syncwarp();
       const uint32_t a = max(s, c), b = min(e, c + n);
-      for (uint32_t i = a; i < b; i++) acc = __fadd_rn(acc, __fmul_rn(sv[i - c], qs[sc[i - c]]));
+      for (uint32_t i = a; i < b; i++) acc = __fadd_rn(acc, sp[i - c]);
       __syncwarp();
     }
     if (r < rows) keys[r] = key_f32(acc);
@@ -1175,19 +1179,30 @@ __global__ void k_filter_keys(const uint32_t* __restrict__ keys, uint32_t rows,
                               uint2* __restrict__ surv, uint32_t cap) {
   const uint32_t th = *thr, lane = threadIdx.x & 31u;
   const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t n_iter = (rows + stride - 1) / stride;  // the same for every lane of a warp
+  const uint32_t n4 = (rows + 3) / 4;                    // groups of four keys (16-byte loads)
+  const uint32_t n_iter = (n4 + stride - 1) / stride;    // the same for every lane of a warp
   for (uint32_t it = 0; it < n_iter; it++) {
-    const uint32_t r = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t key = r < rows ? keys[r] : 0u;
-    const bool hit = r < rows && key >= th;
-    const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
-    if (m) {
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(cnt, (uint32_t)__popc(m));
-      base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      if (hit) {
-        const uint32_t i = base + __popc(m & ((1u << lane) - 1u));
-        if (i < cap) surv[i] = make_uint2(key, r);
+    const uint32_t g = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t k4[4] = {0u, 0u, 0u, 0u};
+    if (g * 4 + 3 < rows) {
+      const uint4 v = __ldcs(reinterpret_cast<const uint4*>(keys) + g);
+      k4[0] = v.x; k4[1] = v.y; k4[2] = v.z; k4[3] = v.w;
+    } else if (g < n4) {
+      for (uint32_t t = 0; t < 4 && g * 4 + t < rows; t++) k4[t] = keys[g * 4 + t];
+    }
+#pragma unroll
+    for (uint32_t t = 0; t < 4; t++) {
+      const uint32_t r = g * 4 + t;
+      const bool hit = r < rows && k4[t] >= th;
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
+      if (m) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(cnt, (uint32_t)__popc(m));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (hit) {
+          const uint32_t i = base + __popc(m & ((1u << lane) - 1u));
+          if (i < cap) surv[i] = make_uint2(k4[t], r);
+        }
       }
     }
   }
