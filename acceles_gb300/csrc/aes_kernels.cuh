@@ -801,12 +801,7 @@ __global__ void __launch_bounds__(kThreadsThr, 2) k_threshold(const uint32_t* __
 #pragma unroll
     for (int u = 0; u < kThrILP; u++) {
       const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
-      const unsigned act = __ballot_sync(0xFFFFFFFFu, i < b);
-      if (i < b) {
-        const uint32_t bin = (v[u] - mn) >> sh1;
-        const unsigned peers = __match_any_sync(act, bin);
-        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
-      }
+      if (i < b) atomicAdd(&hist[(v[u] - mn) >> sh1], 1u);
     }
   }
   __syncthreads();
@@ -831,13 +826,8 @@ __global__ void __launch_bounds__(kThreadsThr, 2) k_threshold(const uint32_t* __
 #pragma unroll
     for (int u = 0; u < kThrILP; u++) {
       const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
-      const bool in = (i < b) && (((v[u] - mn) >> sh1) == b1);
-      const unsigned act = __ballot_sync(0xFFFFFFFFu, in);
-      if (in) {
-        const uint32_t bin = ((v[u] - mn) >> sh2) & ((1u << (sh1 - sh2)) - 1u);
-        const unsigned peers = __match_any_sync(act, bin);
-        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
-      }
+      if ((i < b) && (((v[u] - mn) >> sh1) == b1))
+        atomicAdd(&hist[((v[u] - mn) >> sh2) & ((1u << (sh1 - sh2)) - 1u)], 1u);
     }
   }
   __syncthreads();
