@@ -1005,8 +1005,11 @@ __global__ void k_select(SelectArgs a) {
 // ---------------------------------------------------------------------------------------------
 // k_final: FP32 rescoring of every candidate (sequential over the row's entries in column
 // order, separately rounded multiply and add) and the final Top-K in sort_tuples order.
-// One CTA per query: the K largest (score, row) composites are found by a block radix select,
-// then only those are sorted by a bitonic network in shared memory.
+// One CTA per query. Each warp rescores 32 slots at a time: it loads its rows' entries row by
+// row (lane = entry, coalesced, 8 rows in flight), stages the rounded products in shared memory
+// and each lane then sums its own row's products in entry order. The K largest (score, row)
+// composites are found by a block radix select, then only those are sorted by a bitonic network
+// in shared memory.
 // ---------------------------------------------------------------------------------------------
 struct FinalArgs {
   const uint32_t* csr_ptr;   // [rows+1]
@@ -1021,12 +1024,16 @@ struct FinalArgs {
   const uint32_t* status;    // [nq]; queries with a set status are left to the repair path
 };
 
-// dynamic shared memory of k_final: the query, the composites of all slots, the kp selected
-__host__ __device__ inline size_t final_smem_bytes(uint32_t cols, uint32_t nslots, uint32_t kp) {
-  return (((size_t)cols * 4 + 15) & ~(size_t)15) + (size_t)nslots * 8 + (size_t)kp * 8;
-}
-
 constexpr int kThreadsFinal = 512;  // two CTAs per SM: a 256-query batch runs in one wave
+constexpr int kFinalStageLd = 33;   // staged products: 32 rows x 33 floats per warp
+
+// dynamic shared memory of k_final: the query, the composites of all slots, then one region
+// holding first the per-warp product staging and afterwards the kp selected composites
+__host__ __device__ inline size_t final_smem_bytes(uint32_t cols, uint32_t nslots, uint32_t kp) {
+  const size_t stage = (size_t)(kThreadsFinal / 32) * 32 * kFinalStageLd * 4;
+  const size_t top = (size_t)kp * 8;
+  return (((size_t)cols * 4 + 15) & ~(size_t)15) + (size_t)nslots * 8 + (stage > top ? stage : top);
+}
 
 __global__ void __launch_bounds__(kThreadsFinal, 2) k_final(FinalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1035,35 +1042,46 @@ __global__ void __launch_bounds__(kThreadsFinal, 2) k_final(FinalArgs a) {
   __shared__ uint32_t s_cnt;
   float* qs = reinterpret_cast<float*>(smem);
   uint64_t* comp = reinterpret_cast<uint64_t*>(smem + ((a.cols * 4 + 15) & ~15u));
-  uint64_t* top = comp + a.nslots;
+  uint64_t* top = comp + a.nslots;  // after the rescoring; the product staging before it
   const uint32_t q = blockIdx.x;
   if (a.status && a.status[q]) return;
   const float* x = a.q32 + (size_t)q * a.ld32;
   for (uint32_t j = threadIdx.x; j < a.cols; j += blockDim.x) qs[j] = x[j];
-  for (uint32_t i = threadIdx.x; i < a.kp; i += blockDim.x) top[i] = 0;
   if (threadIdx.x == 0) s_cnt = 0;
   __syncthreads();
   const uint32_t* cr = a.cand + (size_t)q * a.nslots;
-  for (uint32_t i = threadIdx.x; i < a.nslots; i += blockDim.x) {
-    uint64_t c = 0;
-    const uint32_t row = cr[i];
-    if (row != 0xFFFFFFFFu) {
-      uint32_t e = a.csr_ptr[row], e1 = a.csr_ptr[row + 1];
-      float acc = 0.0f;
-      for (; e + 4 <= e1; e += 4) {
-        uint16_t c0 = a.csr_col[e], c1 = a.csr_col[e + 1], c2 = a.csr_col[e + 2], c3 = a.csr_col[e + 3];
-        float v0 = a.csr_val[e], v1 = a.csr_val[e + 1], v2 = a.csr_val[e + 2], v3 = a.csr_val[e + 3];
-        acc = __fadd_rn(acc, __fmul_rn(v0, qs[c0]));
-        acc = __fadd_rn(acc, __fmul_rn(v1, qs[c1]));
-        acc = __fadd_rn(acc, __fmul_rn(v2, qs[c2]));
-        acc = __fadd_rn(acc, __fmul_rn(v3, qs[c3]));
+  {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    float* sp = reinterpret_cast<float*>(top) + warp * (32 * kFinalStageLd);
+    for (uint32_t g = warp * 32; g < a.nslots; g += nwarps * 32) {
+      const uint32_t i = g + lane;
+      const uint32_t row = i < a.nslots ? cr[i] : 0xFFFFFFFFu;
+      uint32_t s = 0, n = 0;
+      if (row != 0xFFFFFFFFu) {
+        s = a.csr_ptr[row];
+        n = a.csr_ptr[row + 1] - s;
       }
-      for (; e < e1; e++) acc = __fadd_rn(acc, __fmul_rn(a.csr_val[e], qs[a.csr_col[e]]));
-      c = ((uint64_t)key_f32(acc) << 32) | row;
+      const uint32_t rounds = (__reduce_max_sync(0xFFFFFFFFu, n) + 31) >> 5;
+      float acc = 0.0f;
+      for (uint32_t r = 0; r < rounds; r++) {
+        const uint32_t o = r * 32 + lane;
+#pragma unroll 8
+        for (int j = 0; j < 32; j++) {
+          const uint32_t sj = __shfl_sync(0xFFFFFFFFu, s, j), nj = __shfl_sync(0xFFFFFFFFu, n, j);
+          float p = 0.0f;
+          if (o < nj) p = __fmul_rn(__ldg(a.csr_val + sj + o), qs[__ldg(a.csr_col + sj + o)]);
+          sp[j * kFinalStageLd + lane] = p;
+        }
+        __syncwarp();
+        const uint32_t m = n > r * 32 ? min(n - r * 32, 32u) : 0u;
+        for (uint32_t e = 0; e < m; e++) acc = __fadd_rn(acc, sp[lane * kFinalStageLd + e]);
+        __syncwarp();
+      }
+      if (i < a.nslots) comp[i] = row != 0xFFFFFFFFu ? ((uint64_t)key_f32(acc) << 32) | row : 0ull;
     }
-    comp[i] = c;
   }
   __syncthreads();
+  for (uint32_t i = threadIdx.x; i < a.kp; i += blockDim.x) top[i] = 0;
   // composites of filled slots are unique (rows are); empty slots are 0 and never selected
   const uint32_t need = min(a.k, a.nslots);
   const uint64_t tau = block_select_tau([&](uint32_t i) -> uint64_t { return comp[i]; }, a.nslots,
