@@ -45,13 +45,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(name):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+def profile_number(name, key):
+    """A `key: number` line of a committed ncu summary, if any."""
     p = os.path.join(REPO, "profiles", name)
     if not os.path.exists(p):
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", open(p).read())
-    return int(m.group(1)) if m else None
+    m = re.search(re.escape(key) + r":\s*([0-9.]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def profile_traffic(name):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    v = profile_number(name, "traffic_bytes_per_launch")
+    return int(v) if v is not None else None
 
 
 class ClockSampler:
@@ -386,6 +392,22 @@ def main():
     plain_achieved = plain_alg / (plain_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = profile_traffic("cand_batch_10Mx1024_b8.md")
+    # the batched pass is bound by instruction issue, not HBM: warp instructions per group of
+    # four entries (ncu instruction count of the capture) x the groups of one launch, over the
+    # live launch time at the sampled SM clock; an SM issues at most 4 warp instructions a cycle
+    issue = None
+    ipg = profile_number("cand_batch_10Mx1024_b8.md", "warp_instructions_per_group")
+    if ipg:
+        groups = info["tiles"] * 32 * (511 // (BITS + 11)) // 4
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+        if mhz:
+            ipl = ipg * groups
+            ach = ipl / (cand_ms / 1e3 * mhz * 1e6 * sms)
+            issue = {"bound": "issue", "unit": "warp instructions per SM cycle", "achieved": ach,
+                     "peak": 4.0, "frac": ach / 4.0, "instructions_per_launch": ipl,
+                     "instructions_per_group": ipg, "groups_per_launch": groups,
+                     "sm_mhz": mhz, "sms": sms}
     plain_traffic = profile_traffic("cand_pass_10Mx1024_b8.md")
 
     # end to end through the host-buffer C ABI (batched engine)
@@ -474,7 +496,8 @@ def main():
                          "kernel": "k_cand_batch<8,signed,FILTER> (128 queries per pass)",
                          "limiter": "CUDA-core integer issue (gathers, byte transposes, dp4a); "
                                     "one matrix read serves 128 queries",
-                         "alg_bytes_per_launch": alg_bytes, "launch_ms": cand_ms},
+                         "alg_bytes_per_launch": alg_bytes, "launch_ms": cand_ms,
+                         "issue": issue},
             "plain_roofline": {"bound": "hbm", "achieved": plain_achieved, "peak": peak,
                                "unit": "GB/s", "frac": plain_achieved / peak,
                                "traffic": plain_traffic, "kernel": "k_cand_plain<8,signed,FILTER>",
