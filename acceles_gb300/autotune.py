@@ -8,8 +8,11 @@ batched sparse-query workload it was written for.
    (score desc, row desc) order) on at least `target` of the sample queries.  The rescoring
    is exact, so a query whose recall@K is 1 has an identical Top-K, and with split 1 a larger
    CK only adds candidates: the first CK that reaches the target is the smallest.
-2. Sample stride and batch tile: for each split's CK, every (stride, tile) of the grid is
-   timed on the sample batch (wall time of aes_run, repairs included); the fastest wins.
+2. Sample stride and candidate pass: for each split's CK, every (stride, pass) of the grid is
+   timed on the sample batch (wall time of aes_run, repairs included); the fastest wins.  The
+   passes are the plain one (one query per matrix read), the dp4a batched one (128 queries per
+   read) and, for 4-bit matrices created with AES_FLAG_TENSOR, the tensor-core batched one
+   (FP8 tcgen05 products of 128-row tiles; same results).
 
 Every trial re-plans the handle with aes_retune; the packed matrix stays resident.
 
@@ -62,9 +65,13 @@ def _time_runs(eng, queries, k, reps):
     return best, st["repaired"]
 
 
+PASSES = ((1, False), (128, False), (128, True))  # (batch_tile, tensor cores)
+
+
 def tune(eng: E.SpMV, queries, k, ck_ladder=CK_LADDER, splits=(1,), strides=(0, 16, 64, 256),
-         tiles=(1, 128), target=1.0, reps=3, log=None):
-    """Choose CK, split, sample stride and batch tile for `queries` (FP32 [nq, cols]) at K=k.
+         passes=PASSES, target=1.0, reps=3, log=None):
+    """Choose CK, split, sample stride and candidate pass for `queries` (FP32 [nq, cols]) at
+    K=k.  The returned params hold batch_tile and flags (AES_FLAG_TENSOR or 0).
 
     Returns {"params": chosen aes_params fields, "ck_trials": [...], "time_trials": [...],
     "exact": the FP32-only Top-K rows of the sample}.  The handle is left retuned to the
@@ -72,7 +79,8 @@ def tune(eng: E.SpMV, queries, k, ck_ladder=CK_LADDER, splits=(1,), strides=(0, 
     """
     Q = np.ascontiguousarray(np.atleast_2d(queries), np.float32)
     nq = Q.shape[0]
-    eng.retune(max_batch=nq, k_max=max(k, 1))
+    base = eng.params.flags & ~E.FLAG_TENSOR
+    eng.retune(max_batch=nq, k_max=max(k, 1), flags=base)
     eng.Q_reset(Q)
     exact, _, _ = eng.run_exact(k=k)
 
@@ -100,24 +108,28 @@ def tune(eng: E.SpMV, queries, k, ck_ladder=CK_LADDER, splits=(1,), strides=(0, 
     time_trials = []
     best = None
     for split, ck in chosen_ck.items():
-        for tile in tiles:
+        for tile, tensor in passes:
             if tile == 128 and nq < 16:
                 continue
+            flags = base | (E.FLAG_TENSOR if tensor else 0)
             for stride in strides:
                 eng.retune(ck=ck, split=split, max_batch=nq, batch_tile=tile,
-                           sample_stride=stride)
+                           sample_stride=stride, flags=flags)
+                if tensor and not eng.info()["tensor_tiles"]:
+                    break  # no tensor-core layout for this matrix or split
                 sec, repaired = _time_runs(eng, Q, k, reps)
-                row = {"split": split, "ck": ck, "batch_tile": tile, "sample_stride": stride,
-                       "ms_per_query": sec * 1e3 / nq, "repaired": int(repaired)}
+                row = {"split": split, "ck": ck, "batch_tile": tile, "tensor": tensor,
+                       "sample_stride": stride, "ms_per_query": sec * 1e3 / nq,
+                       "repaired": int(repaired)}
                 time_trials.append(row)
                 if log:
                     log(row)
                 if best is None or row["ms_per_query"] < best["ms_per_query"]:
                     best = row
-    eng.retune(ck=best["ck"], split=best["split"], max_batch=nq, batch_tile=best["batch_tile"],
-               sample_stride=best["sample_stride"])
     params = {"ck": best["ck"], "split": best["split"], "batch_tile": best["batch_tile"],
-              "sample_stride": best["sample_stride"]}
+              "sample_stride": best["sample_stride"],
+              "flags": base | (E.FLAG_TENSOR if best["tensor"] else 0)}
+    eng.retune(max_batch=nq, **params)
     return {"params": params, "ck_trials": ck_trials, "time_trials": time_trials,
             "exact": exact}
 
@@ -146,8 +158,11 @@ def main():
     peak = 6800.0
     pk = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
                       "MEASURED_PEAKS.json")
+    bf16 = 1944.7  # TFLOP/s; FP8 dense is taken as twice the measured bf16 rate
     if os.path.exists(pk):
-        peak = float(json.load(open(pk))["hbm_gbs"])
+        mp = json.load(open(pk))
+        peak = float(mp["hbm_gbs"])
+        bf16 = float(mp.get("bf16_tflops", bf16))
     lines = []
 
     def emit(d):
@@ -160,7 +175,7 @@ def main():
     t0 = time.perf_counter()
     eng = E.SpMV(args.rows, args.cols, ptr=ptr, col=col, val=val, bits=4,
                  quant=E.QUANT_UNSIGNED_ROW, split=1, ck=1024, k_max=args.k,
-                 max_batch=args.queries, flags=E.FLAG_GRAPHS)
+                 max_batch=args.queries, flags=E.FLAG_GRAPHS | E.FLAG_TENSOR)
     t_build = time.perf_counter() - t0
     info = eng.info()
     emit({"matrix": f"{args.rows}x{args.cols} gamma(2, mean 32) cap 512, U(0,1), 4-bit per-row "
@@ -176,7 +191,9 @@ def main():
     # measure the chosen configuration on the workload's own queries
     Q = sparse_queries(args.queries * 2, args.cols, args.seed + 2)
     nq = args.queries
-    eng.retune(max_batch=nq, flags=E.FLAG_GRAPHS, **prm)
+    tflag = prm["flags"] & E.FLAG_TENSOR
+    run_prm = {k: v for k, v in prm.items() if k != "flags"}
+    eng.retune(max_batch=nq, flags=E.FLAG_GRAPHS | tflag, **run_prm)
     for s in range(args.warmup):
         eng.Q_reset(Q[(s % 2) * nq:(s % 2 + 1) * nq])
         eng(k=args.k)
@@ -190,18 +207,27 @@ def main():
     qps_dev = args.steps * nq / (dev_ns / 1e9)
     qps_e2e = args.steps * nq / wall
     # candidate-pass launch time, profiled outside graphs
-    eng.retune(max_batch=nq, flags=E.FLAG_PROFILE, **prm)
+    eng.retune(max_batch=nq, flags=E.FLAG_PROFILE | tflag, **run_prm)
     eng.Q_reset(Q[:nq])
     eng(k=args.k)
     eng.stats(reset=True)
     eng(k=args.k)
     stp = eng.stats(reset=True)
     launch_ms = stp["cand_ms"] / max(stp["cand_timed"], 1)
-    alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + args.cols * (128 if prm["batch_tile"] == 128 else 1)
+    kpad = (args.cols + 31) // 32 * 32
+    rtiles = (args.rows + 127) // 128
+    if tflag:
+        # tensor-core pass: 4-byte entries, chunk offsets, the e4m3 query operand; dense FP8
+        # products of every 128-row tile with the 128 queries
+        alg = info["quantized_nnz"] * 4 + (rtiles * ((kpad + 255) // 256) + 1) * 4 + 128 * kpad
+        flops = 2.0 * rtiles * 128 * 128 * kpad
+    else:
+        alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + args.cols * (128 if prm["batch_tile"] == 128 else 1)
+        flops = None
     gbs = alg / (launch_ms / 1e3) / 1e9
     # recall of the measured queries against the FP32-only Top-K
     idx, _ = eng.read_topk()
-    eng.retune(max_batch=nq, flags=0, **prm)
+    eng.retune(max_batch=nq, flags=0, **run_prm)
     eng.Q_reset(Q[:nq])
     exact, _, _ = eng.run_exact(k=args.k)
     rec = _recall(idx, exact, args.k)
@@ -209,7 +235,10 @@ def main():
           "steps": args.steps, "qps_device": qps_dev, "qps_e2e_host_buffers": qps_e2e,
           "ms_per_step_device": dev_ns / 1e6 / args.steps, "repaired": st["repaired"],
           "cand_pass": {"launch_ms": launch_ms, "alg_bytes": alg, "gbs": gbs,
-                        "frac_of_measured_hbm": gbs / peak},
+                        "frac_of_measured_hbm": gbs / peak, "tensor_cores": bool(tflag),
+                        "dense_tflops": (flops / (launch_ms / 1e3) / 1e12) if flops else None,
+                        "frac_of_fp8_dense": ((flops / (launch_ms / 1e3) / 1e12) / (2 * bf16))
+                        if flops else None},
           "recall_at_k_mean": float(rec.mean()), "frac_identical_to_fp32_exact": float(np.mean(rec == 1.0)),
           "params": prm})
     if args.json:

@@ -22,6 +22,7 @@
 #include "aes_host.hpp"
 #include "aes_kernels.cuh"
 #include "aes_batch.cuh"
+#include "aes_tc.cuh"
 
 namespace aes {
 const char* last_error_cstr();
@@ -102,6 +103,11 @@ struct Engine {
   uint4* d_tiles = nullptr;
   uint32_t* d_tile_rowbase = nullptr;
   float* d_rowscale = nullptr;
+  // tensor-core layout of a 4-bit matrix (AES_FLAG_TENSOR at creation)
+  uint32_t* d_tc_ptr = nullptr;
+  uint32_t* d_tc_ent = nullptr;
+  uint32_t tc_nch = 0, tc_rtiles = 0;
+  bool tc_ready = false;
   uint32_t* d_csr_ptr = nullptr;
   uint16_t* d_csr_col = nullptr;
   float* d_csr_val = nullptr;
@@ -182,6 +188,10 @@ struct Engine {
   int batch_warps_n = 0, batch_grid = 0;
   size_t batch_smem = 0;
   uint32_t batch_mode = 0;        // 0 auto, 1 never, else always
+  bool use_tc = false;            // batched candidate pass on the tensor cores
+  uint8_t* d_qtab_tc = nullptr;   // [blocks][tc_qtab_bytes(cols)] e4m3 query operands
+  size_t tc_smem = 0;
+  int tc_grid = 0;
   bool last_batched = false;
   std::vector<uint32_t> h_tile_rowbase;  // host copy: sample geometry is derived from it
   size_t bytes = 0, mat_bytes = 0, cfg_bytes = 0;
@@ -259,8 +269,73 @@ struct Engine {
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y = 1);
   int run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s);
+  int run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s);
+  int prof_open(cudaStream_t s);
+  int prof_close(cudaStream_t s);
   int collect_profile();
+  // the tensor-core pass serves a configuration: 4-bit layout built, flag set, thresholds of
+  // every partition in shared memory, batched passes allowed
+  bool tc_usable(const aes_params& p, uint32_t S) const {
+    return tc_ready && (p.flags & AES_FLAG_TENSOR) && S <= kTcMaxSplit && p.batch_tile != 1 &&
+           tc_smem_bytes(cols, S) <= (size_t)smem_optin;
+  }
 };
+
+// CUDA events around one full candidate-pass launch (AES_FLAG_PROFILE)
+int Engine::prof_open(cudaStream_t s) {
+  if (prof_used + 2 > prof_ev.size()) {
+    if (prof_ev.size() >= 8192) {
+      int rc = collect_profile();
+      if (rc) return rc;
+    } else {
+      for (int i = 0; i < 256; i++) {
+        cudaEvent_t ev;
+        AES_CK(cudaEventCreate(&ev));
+        prof_ev.push_back(ev);
+      }
+    }
+  }
+  AES_CK(cudaEventRecord(prof_ev[prof_used], s));
+  return AES_OK;
+}
+int Engine::prof_close(cudaStream_t s) {
+  AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
+  prof_used += 2;
+  return AES_OK;
+}
+
+// Batched candidate pass of one block of <= 128 queries on the tensor cores (aes_tc.cuh); its
+// query blocks are those of the dp4a pass, whose sample pass it shares
+static_assert(kTcQ == kBatchQ, "tensor-core and dp4a passes use the same query blocks");
+int Engine::run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
+  TcArgs a{};
+  a.ent = d_tc_ent;
+  a.ptr = d_tc_ptr;
+  a.n_rtiles = tc_rtiles;
+  a.nch = tc_nch;
+  a.kpad = tc_kpad(cols);
+  a.n_rows = rows;
+  a.qt = d_qtab_tc + (size_t)blk * tc_qtab_bytes(cols);
+  a.q0 = blk * kTcQ;
+  a.nq = nq_blk;
+  a.rowscale = d_rowscale;
+  a.split = split;
+  a.slice = slice;
+  a.thr = d_thr;
+  a.cnt = d_cnt;
+  a.surv = d_surv;
+  a.cap = cap;
+  a.status = d_status;
+  const bool prof = (prm.flags & AES_FLAG_PROFILE) != 0;
+  int rc = prof ? prof_open(s) : AES_OK;
+  if (rc) return rc;
+  k_cand_tc<<<tc_grid, kTcThreads, tc_smem, s>>>(a);
+  AES_CK(cudaGetLastError());
+  if (prof && (rc = prof_close(s))) return rc;
+  n_launch++;
+  n_cand++;
+  return AES_OK;
+}
 
 int Engine::collect_profile() {
   for (size_t i = 0; i + 1 < prof_used; i += 2) {
@@ -368,6 +443,7 @@ int Engine::plan_config(const aes_params& p, Config* c) const {
   plan += maxB * (ld32 * 4ull + ld8 + S * 8ull + (size_t)S * c->cap * 8 + c->nslots * 8ull + 4 +
                   p.k_max * 8ull);
   plan += nblk * batch_qtab_words(cols) * 4;
+  if (tc_usable(p, S)) plan += nblk * tc_qtab_bytes(cols);
   plan += p.k_max * 8ull;
   c->plan = plan;
 
@@ -411,6 +487,8 @@ int Engine::apply_config(const Config& c) {
   AES_AL(d_out_idx, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_out_score, (size_t)maxB * std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_qtab, (size_t)((maxB + kBatchQ - 1) / kBatchQ) * batch_qtab_words(cols));
+  use_tc = tc_usable(p, split);
+  if (use_tc) AES_AL(d_qtab_tc, (size_t)((maxB + kTcQ - 1) / kTcQ) * tc_qtab_bytes(cols));
   AES_AL(d_exact_cand, std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_exact_key, std::max<uint32_t>(p.k_max, 1));
   AES_AL(d_exact_aux, 4);
@@ -438,6 +516,12 @@ int Engine::apply_config(const Config& c) {
     AES_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &occb, (const void*)pick_batch((int)bits, sgn, MODE_FILTER), batch_warps_n * 32, batch_smem));
     batch_grid = std::max(1, occb) * sm_count;
+  }
+  if (use_tc) {  // one CTA per SM (its shared memory), persistent over the 128-row tiles
+    tc_smem = tc_smem_bytes(cols, split);
+    tc_grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)sm_count, tc_rtiles));
+  } else {
+    d_qtab_tc = nullptr;
   }
   {
     uint32_t kp = 1;
@@ -485,13 +569,17 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   tiles = pm.tiles;
   if (tiles >= 0xFFFFFFFFull) return fail(AES_ERR_UNSUPPORTED, "matrix too large");
   h_tile_rowbase = pm.tile_rowbase;
+  tc_ready = !pm.tc_ptr.empty();
+  tc_nch = pm.tc_nch;
+  tc_rtiles = (uint32_t)((rows + kTcRows - 1) / kTcRows);
+  const size_t tc_bytes = tc_ready ? (pm.tc_ptr.size() + pm.tc_ent.size()) * 4 : 0;
 
   Config c;
   rc = plan_config(p, &c);
   if (rc) return rc;
 
   // ---- memory plan and admission: nothing is allocated unless all of it fits ---------------
-  const size_t plan = matrix_plan(tiles, rows, nnz, quant) + c.plan;
+  const size_t plan = matrix_plan(tiles, rows, nnz, quant) + tc_bytes + c.plan;
   if (p.mem_limit && plan > p.mem_limit)
     return fail(AES_ERR_NOMEM, "matrix needs " + std::to_string(plan) +
                                    " device bytes, over the handle limit " +
@@ -511,6 +599,10 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_AL(d_csr_col, std::max<uint64_t>(nnz, 1));
   AES_AL(d_csr_val, std::max<uint64_t>(nnz, 1));
   AES_AL(d_allkeys, rows);
+  if (tc_ready) {
+    AES_AL(d_tc_ptr, pm.tc_ptr.size());
+    AES_AL(d_tc_ent, std::max<size_t>(pm.tc_ent.size(), 1));
+  }
 #undef AES_AL
 
   // ---- upload -----------------------------------------------------------------------------------
@@ -528,6 +620,11 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     AES_CK(cudaMemcpy(d_csr_col, col16.data(), nnz * 2, cudaMemcpyHostToDevice));
     AES_CK(cudaMemcpy(d_csr_val, m.val.data(), nnz * 4, cudaMemcpyHostToDevice));
   }
+  if (tc_ready) {
+    AES_CK(cudaMemcpy(d_tc_ptr, pm.tc_ptr.data(), pm.tc_ptr.size() * 4, cudaMemcpyHostToDevice));
+    if (!pm.tc_ent.empty())
+      AES_CK(cudaMemcpy(d_tc_ent, pm.tc_ent.data(), pm.tc_ent.size() * 4, cudaMemcpyHostToDevice));
+  }
 
   // the shared-memory limit is an attribute of the kernel, shared by every handle: raise it to
   // the device maximum (less the kernel's static shared memory) once, not to this handle's size
@@ -543,6 +640,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   for (int mode = 0; mode < 2; mode++)
     AES_CK(raise_smem((const void*)pick_batch((int)bits, sgn, mode)));
   AES_CK(raise_smem((const void*)k_final));
+  if (tc_ready) AES_CK(raise_smem((const void*)k_cand_tc));
   rc = apply_config(c);
   if (rc) return rc;
   AES_CK(cudaDeviceSynchronize());
@@ -619,27 +717,11 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y) {
   }
   grid = std::max(grid, 1);
   const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
-  if (prof) {
-    if (prof_used + 2 > prof_ev.size()) {
-      if (prof_ev.size() >= 8192) {
-        int rc = collect_profile();
-        if (rc) return rc;
-      } else {
-        for (int i = 0; i < 256; i++) {
-          cudaEvent_t ev;
-          AES_CK(cudaEventCreate(&ev));
-          prof_ev.push_back(ev);
-        }
-      }
-    }
-    AES_CK(cudaEventRecord(prof_ev[prof_used], s));
-  }
+  int rc = prof ? prof_open(s) : AES_OK;
+  if (rc) return rc;
   pick_plain((int)bits, sgn, mode)<<<dim3(grid, nq_y), plain_threads((int)bits), plain_smem, s>>>(a);
   AES_CK(cudaGetLastError());
-  if (prof) {
-    AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
-    prof_used += 2;
-  }
+  if (prof && (rc = prof_close(s))) return rc;
   n_launch++;
   if (mode != MODE_SAMPLE) n_cand++;
   return AES_OK;
@@ -671,27 +753,11 @@ int Engine::run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
     grid = std::min<int>(grid, (int)((n_sample_tiles + batch_warps_n - 1) / batch_warps_n));
   grid = std::max(grid, 1);
   const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
-  if (prof) {
-    if (prof_used + 2 > prof_ev.size()) {
-      if (prof_ev.size() >= 8192) {
-        int rc = collect_profile();
-        if (rc) return rc;
-      } else {
-        for (int i = 0; i < 256; i++) {
-          cudaEvent_t ev;
-          AES_CK(cudaEventCreate(&ev));
-          prof_ev.push_back(ev);
-        }
-      }
-    }
-    AES_CK(cudaEventRecord(prof_ev[prof_used], s));
-  }
+  int rc = prof ? prof_open(s) : AES_OK;
+  if (rc) return rc;
   pick_batch((int)bits, sgn, mode)<<<grid, batch_warps_n * 32, batch_smem, s>>>(a);
   AES_CK(cudaGetLastError());
-  if (prof) {
-    AES_CK(cudaEventRecord(prof_ev[prof_used + 1], s));
-    prof_used += 2;
-  }
+  if (prof && (rc = prof_close(s))) return rc;
   n_launch++;
   if (mode != MODE_SAMPLE) n_cand++;
   return AES_OK;
@@ -714,6 +780,12 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
           d_q8, ld8, cols, b * kBatchQ, nb, d_qtab + (size_t)b * batch_qtab_words(cols));
       AES_CK(cudaGetLastError());
       n_launch++;
+      if (use_tc) {
+        k_qtable_tc<<<(kTcQ * tc_kpad(cols) + 255) / 256, 256, 0, s>>>(
+            d_q8, ld8, cols, b * kTcQ, nb, d_qtab_tc + (size_t)b * tc_qtab_bytes(cols));
+        AES_CK(cudaGetLastError());
+        n_launch++;
+      }
       int rc = run_batch(MODE_SAMPLE, b, nb, s);
       if (rc) return rc;
     }
@@ -739,7 +811,7 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   if (batched) {
     for (uint32_t b = 0; b < nblk; b++) {
       const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
-      int rc = run_batch(MODE_FILTER, b, nb, s);
+      int rc = use_tc ? run_tc(b, nb, s) : run_batch(MODE_FILTER, b, nb, s);
       if (rc) return rc;
     }
   } else {
@@ -831,6 +903,8 @@ int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cud
   for (uint32_t q = 0; q < nq; q++) {
     if (h_status[q] & ST_QUERY) return fail(AES_ERR_QUERY, "query " + std::to_string(q) +
                                                " has negative entries under an unsigned quantiser");
+    if (h_status[q] & ST_DEVICE)
+      return fail(AES_ERR_CUDA, "tensor-core candidate pass: a bounded wait gave up");
   }
   for (uint32_t q = 0; q < nq; q++) {
     if (!(h_status[q] & (ST_OVERFLOW | ST_MISS))) continue;
@@ -1034,6 +1108,7 @@ int aes_get_info(const aes_handle* h, aes_info* info) {
   info->sample_rows = e.n_sample_rows;
   info->max_batch = e.maxB;
   info->batch_tile = e.batch_mode == 1 ? 1 : aes::dev::kBatchQ;
+  info->tensor_tiles = e.use_tc ? 1u : 0u;
   return AES_OK;
 }
 

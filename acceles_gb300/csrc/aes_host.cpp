@@ -9,6 +9,7 @@
 //   Q_packet_coo(_partition)  src/fpga/src/host_spmv_ucsr.cpp:278-319, :388-425
 //   Q_write_block_x/y/val     src/fpga/src/ip/fpga_utils.hpp:438-503
 #include "aes_host.hpp"
+#include "aes_tc_layout.h"
 
 #include <algorithm>
 #include <cmath>
@@ -141,6 +142,59 @@ struct Bits512 {
     if (s + width > 64) w[k + 1] |= v >> (64 - s);
   }
 };
+
+// Tensor-core layout of a 4-bit matrix (PackedMatrix::tc_*).  Left empty when a row holds a
+// column twice (the dense tile would keep one of the two values) or nnz needs 64-bit offsets.
+static void build_tc_layout(const std::vector<uint64_t>& qptr, const std::vector<uint16_t>& qcol,
+                            const std::vector<int8_t>& qval, PackedMatrix* out) {
+  const uint32_t rows = out->rows;
+  const uint64_t qnnz = qptr[rows];
+  if (qnnz > 0xFFFFFFFFull) return;
+  const uint32_t nch = tc_nchunks(out->cols);
+  const uint64_t nt = ((uint64_t)rows + kTcRows - 1) / kTcRows;
+  std::vector<uint32_t> cnt(nt * nch + 1, 0);
+  std::vector<char> dup(nt, 0);
+  parallel_for(nt, 64, [&](uint64_t b, uint64_t e) {
+    for (uint64_t t = b; t < e; t++) {
+      const uint64_t r1 = std::min<uint64_t>(rows, (t + 1) * kTcRows);
+      for (uint64_t r = t * kTcRows; r < r1; r++) {
+        std::vector<uint64_t> seen;
+        for (uint64_t i = qptr[r]; i < qptr[r + 1]; i++) {
+          cnt[t * nch + qcol[i] / kTcChunkK]++;
+          // columns are in order within a row unless the input holds duplicates
+          if (i > qptr[r] && qcol[i] <= qcol[i - 1]) {
+            if (seen.empty()) {
+              seen.assign(16, 0);
+              for (uint64_t j = qptr[r]; j < i; j++) seen[qcol[j] >> 6] |= 1ull << (qcol[j] & 63);
+            }
+            if (seen[qcol[i] >> 6] >> (qcol[i] & 63) & 1) dup[t] = 1;
+          }
+          if (!seen.empty()) seen[qcol[i] >> 6] |= 1ull << (qcol[i] & 63);
+        }
+      }
+    }
+  });
+  for (uint64_t t = 0; t < nt; t++)
+    if (dup[t]) return;
+  out->tc_ptr.assign(nt * nch + 1, 0);
+  for (uint64_t j = 0; j < nt * nch; j++) out->tc_ptr[j + 1] = out->tc_ptr[j] + cnt[j];
+  out->tc_ent.assign(qnnz, 0);
+  parallel_for(nt, 64, [&](uint64_t b, uint64_t e) {
+    std::vector<uint32_t> fill(nch);
+    for (uint64_t t = b; t < e; t++) {
+      for (uint32_t c = 0; c < nch; c++) fill[c] = out->tc_ptr[t * nch + c];
+      const uint64_t r1 = std::min<uint64_t>(rows, (t + 1) * kTcRows);
+      for (uint64_t r = t * kTcRows; r < r1; r++) {
+        for (uint64_t i = qptr[r]; i < qptr[r + 1]; i++) {
+          const uint32_t c = qcol[i] / kTcChunkK, k = qcol[i] % kTcChunkK;
+          out->tc_ent[fill[c]++] = tc_off((uint32_t)(r - t * kTcRows), k) |
+                                   ((uint32_t)e4m3_small((int)qval[i]) << 16);
+        }
+      }
+    }
+  });
+  out->tc_nch = nch;
+}
 
 int quantize_and_pack(const HostCSR& m, const aes_params& p, PackedMatrix* out) {
   const uint32_t rows = m.rows;
@@ -316,6 +370,7 @@ int quantize_and_pack(const HostCSR& m, const aes_params& p, PackedMatrix* out) 
   for (uint64_t t = 0; t < tiles; t++) out->tile_rowbase[t + 1] = out->tile_rowbase[t] + tile_flags[t];
   if (rows && out->tile_rowbase[tiles] != rows - 1)
     return fail(AES_ERR_INVALID, "internal: packed row count mismatch");
+  if (bits == 4 && (p.flags & AES_FLAG_TENSOR)) build_tc_layout(qptr, qcol, qval, out);
   return AES_OK;
 }
 

@@ -47,6 +47,12 @@ struct PackedMatrix {
   std::vector<uint8_t> tile_bytes;
   std::vector<uint32_t> tile_rowbase;  // flags set in all packets before tile t; size tiles+1
   std::vector<float> rowscale;         // AES_QUANT_UNSIGNED_ROW only
+  // Tensor-core layout (B = 4 with AES_FLAG_TENSOR and no duplicate (row, col)): the entries of
+  // each 128-row tile grouped by 256-column chunk, tile-major; an entry is its byte offset in
+  // the chunk operand (tc_off of the row in the tile and the column in the chunk) | its e4m3
+  // value << 16.  tc_ptr[t * tc_nch + c] is the first entry of (tile t, chunk c).
+  std::vector<uint32_t> tc_ptr, tc_ent;
+  uint32_t tc_nch = 0;
 };
 
 // Quantise (quantify_util.py:8-28 or the per-row variant), drop zero results

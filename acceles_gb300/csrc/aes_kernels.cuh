@@ -35,6 +35,7 @@ enum Mode : int { MODE_FILTER = 0, MODE_SAMPLE = 1, MODE_ALL = 2 };
 constexpr uint32_t ST_OVERFLOW = 1u;  // survivors exceeded the buffer
 constexpr uint32_t ST_MISS = 2u;      // fewer survivors than candidates needed
 constexpr uint32_t ST_QUERY = 4u;     // query rejected by the quantiser
+constexpr uint32_t ST_DEVICE = 8u;    // a bounded wait on the tensor pipe gave up
 
 __host__ __device__ constexpr int packet_elems(int B) { return 511 / (B + 11); }
 

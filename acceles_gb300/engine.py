@@ -45,6 +45,7 @@ EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", 
 
 FLAG_PROFILE = 1
 FLAG_GRAPHS = 2
+FLAG_TENSOR = 4  # 4-bit matrices: batched candidate pass on the tensor cores (tcgen05, FP8)
 
 
 class AesError(RuntimeError):
@@ -78,10 +79,10 @@ class Info(ctypes.Structure):
                 ("ck", ctypes.c_uint32), ("ck_effective", ctypes.c_uint32),
                 ("sample_tiles", ctypes.c_uint32), ("sample_rows", ctypes.c_uint32),
                 ("max_batch", ctypes.c_uint32), ("batch_tile", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("tensor_tiles", ctypes.c_uint32)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 _lib = None

@@ -61,7 +61,7 @@ typedef struct aes_params {
   uint32_t sample_stride; /* threshold sample: one 32-packet tile in this many (0 = auto) */
   uint32_t batch_tile;    /* queries per matrix pass in the batched kernel (0 = auto) */
   int32_t device;         /* CUDA device ordinal */
-  uint32_t flags;         /* reserved, 0 */
+  uint32_t flags;         /* AES_FLAG_* bits */
   uint64_t seed;          /* seed of the empty-row rule (check_empty_rows is unseeded) */
   uint64_t mem_limit;     /* device bytes this handle may allocate; 0 = no limit */
 } aes_params;
@@ -71,6 +71,12 @@ typedef struct aes_params {
 #define AES_FLAG_GRAPHS 2u  /* replay each batch's launch sequence as a CUDA graph (captured once
                                per set of buffers, batch size and K); profiling events are
                                not recorded inside graphs */
+#define AES_FLAG_TENSOR 4u  /* 4-bit matrices: lay the quantised entries out for the tensor
+                               cores at creation (4 B per entry) and run the batched candidate
+                               pass as FP8 tcgen05 products of 128-row tiles; the integers are
+                               exact in FP8 and the scores exact in FP32, so results equal the
+                               dp4a pass.  Ignored for 6- and 8-bit matrices, for matrices with
+                               duplicate (row, col) entries and for split > 32 */
 
 typedef struct aes_stats {
   uint64_t launches;       /* kernels launched by the engine since the last reset */
@@ -86,7 +92,8 @@ typedef struct aes_info {
   uint64_t packet_bytes;  /* Ultra-CSR bytes streamed by one full candidate pass */
   uint64_t device_bytes;  /* device memory held by the handle */
   uint32_t split, ck, ck_effective, sample_tiles;
-  uint32_t sample_rows, max_batch, batch_tile, reserved;
+  uint32_t sample_rows, max_batch, batch_tile;
+  uint32_t tensor_tiles;  /* 1 when the batched candidate pass runs on the tensor cores */
 } aes_info;
 
 /* Defaults: bits 6, AES_QUANT_SYM_GLOBAL, AES_QQ_NUMPY, split 32, ck 512, k_max 100

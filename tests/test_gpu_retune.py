@@ -81,12 +81,15 @@ def test_autotune_reaches_target_and_leaves_handle_tuned():
     rows, cols, k = 40000, 1024, 100
     ptr, col, val, m = _setup(rows, cols)
     eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=1, split=1, ck=1024,
-                 k_max=k, max_batch=32)
+                 k_max=k, max_batch=32, flags=E.FLAG_TENSOR)
     Q = AT.sparse_queries(24, cols, 17)
     res = AT.tune(eng, Q, k, ck_ladder=(128, 256, 512, 1024, 2048), splits=(1, 32),
-                  strides=(0, 16), tiles=(1, 128), reps=1)
+                  strides=(0, 16), reps=1)
     prm = res["params"]
     assert eng.info()["split"] == prm["split"]
+    # all three candidate passes were timed; the handle runs the chosen one
+    assert {(t["batch_tile"], t["tensor"]) for t in res["time_trials"]} == set(AT.PASSES)
+    assert eng.info()["tensor_tiles"] == (1 if prm["flags"] & E.FLAG_TENSOR else 0)
     # the chosen configuration reproduces the FP32-only Top-K on every sample query
     eng.Q_reset(Q)
     eng(k=k)
