@@ -137,7 +137,7 @@ __device__ __forceinline__ bool tc_epilogue(const TcArgs& a, uint32_t T, uint32_
     p = part_of(row, S, a.slice);
     if (a.rowscale) rs = __ldg(a.rowscale + row);
   }
-  const uint32_t* th = thr_s + p * kTcQ;
+  const float* thf = reinterpret_cast<const float*>(thr_s) + p * kTcQ;
 #pragma unroll 1
   for (uint32_t cc = 0; cc < 2; cc++) {
     const uint32_t col0 = h * 64u + cc * 32u;
@@ -147,9 +147,10 @@ __device__ __forceinline__ bool tc_epilogue(const TcArgs& a, uint32_t T, uint32_
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const uint32_t q = col0 + j;
-        const int32_t s = __float2int_rn(__uint_as_float(v[j]));
-        const uint32_t key = a.rowscale ? key_f32(__fmul_rn(__int2float_rn(s), rs)) : key_i32(s);
-        if (key >= th[q] && q < a.nq) {
+        const float f = __uint_as_float(v[j]);  // an exact integer score
+        const float x = a.rowscale ? __fmul_rn(f, rs) : f;
+        if (x >= thf[q] && q < a.nq) {
+          const uint32_t key = a.rowscale ? key_f32(x) : key_i32(__float2int_rn(f));
           const size_t qp = (size_t)(a.q0 + q) * S + p;
           const uint32_t i = atomicAdd(a.cnt + qp, 1u);
           if (i < a.cap) a.surv[qp * a.cap + i] = make_uint2(key, row);
@@ -160,6 +161,36 @@ __device__ __forceinline__ bool tc_epilogue(const TcArgs& a, uint32_t T, uint32_
   tc_fence_before();
   return ok;
 }
+
+constexpr int kTcPer = 8;  // entries of a chunk a thread holds in registers (2048 per chunk)
+
+// A thread's share of one chunk's entries: v[u] = entry b + tid + 256 u for tid + 256 u < n
+struct TcEnt {
+  uint32_t v[kTcPer];
+  uint32_t b = 0, n = 0;
+  __device__ __forceinline__ void load(const uint32_t* ent, uint32_t b_, uint32_t n_, uint32_t tid) {
+    b = b_;
+    n = n_;
+#pragma unroll
+    for (int u = 0; u < kTcPer; u++) {
+      const uint32_t i = tid + (uint32_t)u * kTcThreads;
+      v[u] = i < n ? __ldg(ent + b + i) : 0u;
+    }
+  }
+  // writes the entries' e4m3 bytes (or zeros) into a chunk buffer
+  __device__ __forceinline__ void stage(unsigned char* ab, const uint32_t* ent, uint32_t tid,
+                                        bool clear) const {
+#pragma unroll
+    for (int u = 0; u < kTcPer; u++) {
+      const uint32_t i = tid + (uint32_t)u * kTcThreads;
+      if (i < n) ab[v[u] & 0xFFFFu] = clear ? (uint8_t)0 : (uint8_t)(v[u] >> 16);
+    }
+    for (uint32_t i = tid + kTcPer * kTcThreads; i < n; i += kTcThreads) {
+      const uint32_t e = __ldg(ent + b + i);
+      ab[e & 0xFFFFu] = clear ? (uint8_t)0 : (uint8_t)(e >> 16);
+    }
+  }
+};
 
 // One CTA per SM, persistent over row tiles T = blockIdx.x, + gridDim.x, ...
 __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
@@ -178,9 +209,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     for (uint32_t i = tid; i < qbytes / 16u; i += blockDim.x) dst[i] = src[i];
     uint4* z = reinterpret_cast<uint4*>(sa);
     for (uint32_t i = tid; i < 2 * kTcChunkBytes / 16u; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    // thresholds as FP32 bounds on the score (int keys) or on rowscale * score, so that the
+    // comparison needs no conversion: key >= th  <=>  bound <= x for every x the pass produces
     for (uint32_t i = tid; i < S * kTcQ; i += blockDim.x) {
       const uint32_t p = i / kTcQ, q = i % kTcQ;
-      thr_s[i] = q < a.nq ? a.thr[(size_t)(a.q0 + q) * S + p] : 0xFFFFFFFFu;
+      const uint32_t th = q < a.nq ? a.thr[(size_t)(a.q0 + q) * S + p] : 0xFFFFFFFFu;
+      float fb;
+      if (a.rowscale) {  // x >= +0, key(x) = bits(x) | 2^31; NaN bits: never
+        fb = th <= 0x80000000u ? -__int_as_float(0x7f800000) : __uint_as_float(th & 0x7FFFFFFFu);
+      } else {           // |score| < 2^24, exact in FP32
+        const int32_t b = (int32_t)(th ^ 0x80000000u);
+        fb = b > (1 << 24) ? __int_as_float(0x7f800000)
+                           : (b < -(1 << 24) ? -__int_as_float(0x7f800000) : __int2float_rn(b));
+      }
+      thr_s[i] = __float_as_uint(fb);
     }
   }
   if (tid == 0) {
@@ -204,55 +246,89 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
   const uint32_t ep_chunk = a.nch > 1 ? 1u : 0u;  // the chunk after which the previous tile's
                                                   // accumulator is read
+  // Entries move through registers: a thread holds entries tid + 256 u (u < kTcPer) of a chunk,
+  // chunk i in ring set E[i % 4].  Step i clears chunk i - 2 from E[(i + 2) % 4], then loads
+  // chunk i + 2 into it, and stages chunk i (loaded two steps earlier); the row offsets of a
+  // chunk are read four steps before its entries.  The ring has static names (the step is
+  // unrolled four times), so no register copy waits on a load in flight.  Chunks of more than
+  // 256 kTcPer entries read the rest from global memory.
+  const uint32_t ntl = a.n_rtiles > blockIdx.x ? (a.n_rtiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
+  const uint32_t total = ntl * a.nch;  // chunks of this CTA
+  auto chunk_id = [&](uint32_t i) -> uint32_t {
+    return i < total ? (blockIdx.x + (i / a.nch) * gridDim.x) * a.nch + i % a.nch : 0xFFFFFFFFu;
+  };
+  auto ptr_of = [&](uint32_t i, uint32_t& b, uint32_t& e) {
+    const uint32_t j = chunk_id(i);
+    b = j != 0xFFFFFFFFu ? __ldg(a.ptr + j) : 0u;
+    e = j != 0xFFFFFFFFu ? __ldg(a.ptr + j + 1) : 0u;
+  };
+  TcEnt E0, E1, E2, E3;
+  uint32_t P0b, P0e, P1b, P1e, P2b, P2e, P3b, P3e;  // row offsets of chunk i + 2 in P[(i + 2) % 4]
+  {
+    uint32_t b, e;
+    ptr_of(0, b, e);
+    E0.load(a.ent, b, e - b, tid);
+    ptr_of(1, b, e);
+    E1.load(a.ent, b, e - b, tid);
+    ptr_of(2, P2b, P2e);
+    ptr_of(3, P3b, P3e);
+    ptr_of(4, P0b, P0e);
+    ptr_of(5, P1b, P1e);
+  }
   // ok: every bounded wait of this thread succeeded.  The CTA leaves the loop together (the
   // barrier's AND) at the first failure, so a stalled tensor pipe costs one wait, not one per chunk.
   bool ok = true, live = true;
-  uint32_t it = 0, tl = 0, pend0 = 0, pend1 = 0, Tprev = 0;  // pendN: chunk last staged in buffer N
-  for (uint32_t T = blockIdx.x; live && T < a.n_rtiles; T += gridDim.x, tl++) {
-    for (uint32_t c = 0; c < a.nch; c++, it++) {
-      const uint32_t buf = it & 1u;
-      unsigned char* ab = sa + buf * kTcChunkBytes;
-      if (it >= 2) {  // the MMAs of chunk it - 2 have read this buffer: clear its entries
-        ok &= tc_wait(bar_chunk + 8u * buf, ((it - 2) >> 1) & 1u);
-        const uint32_t jp = buf ? pend1 : pend0;
-        for (uint32_t i = a.ptr[jp] + tid; i < a.ptr[jp + 1]; i += blockDim.x)
-          ab[__ldg(a.ent + i) & 0xFFFFu] = 0;
-      }
-      // every clear lands before any write of this chunk (they may share a byte)
-      if (!__syncthreads_and(ok)) {
-        live = false;
-        break;
-      }
-      const uint32_t j = T * a.nch + c;
-      if (buf) pend1 = j; else pend0 = j;
-      for (uint32_t i = a.ptr[j] + tid; i < a.ptr[j + 1]; i += blockDim.x) {
-        const uint32_t e = __ldg(a.ent + i);
-        ab[e & 0xFFFFu] = (uint8_t)(e >> 16);
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tc_fence_before();
-      __syncthreads();
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t nk = min(kTcChunkK, a.kpad - c * kTcChunkK) / 32u;
-        const uint32_t d = tmem + (tl & 1u) * kTcQ;
-        for (uint32_t kk = 0; kk < nk; kk++)
-          tc_mma(d, tc_desc(sa_addr + buf * kTcChunkBytes + kk * 4096u),
-                 tc_desc(sq_addr + (c * 16u + 2u * kk) * 2048u), idesc, (c | kk) != 0);
-        tc_commit(bar_chunk + 8u * buf);
-        if (c == a.nch - 1) tc_commit(bar_acc + 8u * (tl & 1u));
-      }
-      if (tl > 0 && c == ep_chunk)
-        ok &= tc_epilogue(a, Tprev, tmem, (tl - 1) & 1u, bar_acc + 8u * ((tl - 1) & 1u),
-                          ((tl - 1) >> 1) & 1u, thr_s, S);
+  auto step = [&](uint32_t i, TcEnt& cur, TcEnt& old, uint32_t& pb, uint32_t& pe) {
+    const uint32_t tl = i / a.nch, c = i % a.nch;
+    const uint32_t buf = i & 1u;
+    unsigned char* ab = sa + buf * kTcChunkBytes;
+    if (i >= 2) {  // the MMAs of chunk i - 2 have read this buffer: clear its entries
+      ok &= tc_wait(bar_chunk + 8u * buf, ((i - 2) >> 1) & 1u);
+      old.stage(ab, a.ent, tid, true);
     }
-    Tprev = T;
+    // every clear lands before any write of this chunk (they may share a byte)
+    if (!__syncthreads_and(ok)) {
+      live = false;
+      return;
+    }
+    old.load(a.ent, pb, pe - pb, tid);  // chunk i + 2
+    ptr_of(i + 6, pb, pe);
+    cur.stage(ab, a.ent, tid, false);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t nk = min(kTcChunkK, a.kpad - c * kTcChunkK) / 32u;
+      const uint32_t d = tmem + (tl & 1u) * kTcQ;
+      for (uint32_t kk = 0; kk < nk; kk++)
+        tc_mma(d, tc_desc(sa_addr + buf * kTcChunkBytes + kk * 4096u),
+               tc_desc(sq_addr + (c * 16u + 2u * kk) * 2048u), idesc, (c | kk) != 0);
+      tc_commit(bar_chunk + 8u * buf);
+      if (c == a.nch - 1) tc_commit(bar_acc + 8u * (tl & 1u));
+    }
+  };
+  for (uint32_t i = 0; i < total; i++) {
+    switch (i & 3u) {  // static ring names: four inlined copies of the step
+      case 0: step(i, E0, E2, P2b, P2e); break;
+      case 1: step(i, E1, E3, P3b, P3e); break;
+      case 2: step(i, E2, E0, P0b, P0e); break;
+      default: step(i, E3, E1, P1b, P1e); break;
+    }
+    if (!live) break;
+    const uint32_t tl = i / a.nch;
+    if (tl > 0 && i % a.nch == ep_chunk)  // the previous tile's accumulator
+      ok &= tc_epilogue(a, blockIdx.x + (tl - 1) * gridDim.x, tmem, (tl - 1) & 1u,
+                        bar_acc + 8u * ((tl - 1) & 1u), ((tl - 1) >> 1) & 1u, thr_s, S);
   }
-  if (__syncthreads_and(ok) && tl > 0)
-    ok &= tc_epilogue(a, Tprev, tmem, (tl - 1) & 1u, bar_acc + 8u * ((tl - 1) & 1u),
-                      ((tl - 1) >> 1) & 1u, thr_s, S);
+  const uint32_t it = total;
+  if (__syncthreads_and(ok && live) && ntl > 0) {
+    const uint32_t tl = ntl - 1;
+    ok &= tc_epilogue(a, blockIdx.x + tl * gridDim.x, tmem, tl & 1u, bar_acc + 8u * (tl & 1u),
+                      (tl >> 1) & 1u, thr_s, S);
+  }
   // the chunk barriers' last arrivals land before the CTA (and its shared memory) goes away
-  if (__syncthreads_and(ok)) {
+  if (__syncthreads_and(ok && live)) {
     if (it >= 1) ok &= tc_wait(bar_chunk + 8u * ((it - 1) & 1u), ((it - 1) >> 1) & 1u);
     if (it >= 2) ok &= tc_wait(bar_chunk + 8u * ((it - 2) & 1u), ((it - 2) >> 1) & 1u);
   }
