@@ -187,8 +187,8 @@ static void build_tc_layout(const std::vector<uint64_t>& qptr, const std::vector
       for (uint64_t r = t * kTcRows; r < r1; r++) {
         for (uint64_t i = qptr[r]; i < qptr[r + 1]; i++) {
           const uint32_t c = qcol[i] / kTcChunkK, k = qcol[i] % kTcChunkK;
-          out->tc_ent[fill[c]++] = tc_off((uint32_t)(r - t * kTcRows), k) |
-                                   ((uint32_t)e4m3_small((int)qval[i]) << 16);
+          out->tc_ent[fill[c]++] = (tc_off((uint32_t)(r - t * kTcRows), k) << 16) |
+                                   (uint32_t)e4m3_small((int)qval[i]);
         }
       }
     }

@@ -49,8 +49,8 @@ struct PackedMatrix {
   std::vector<float> rowscale;         // AES_QUANT_UNSIGNED_ROW only
   // Tensor-core layout (B = 4 with AES_FLAG_TENSOR and no duplicate (row, col)): the entries of
   // each 128-row tile grouped by 256-column chunk, tile-major; an entry is its byte offset in
-  // the chunk operand (tc_off of the row in the tile and the column in the chunk) | its e4m3
-  // value << 16.  tc_ptr[t * tc_nch + c] is the first entry of (tile t, chunk c).
+  // the chunk operand (tc_off of the row in the tile and the column in the chunk) << 16 | its
+  // e4m3 value.  tc_ptr[t * tc_nch + c] is the first entry of (tile t, chunk c).
   std::vector<uint32_t> tc_ptr, tc_ent;
   uint32_t tc_nch = 0;
 };

@@ -11,6 +11,8 @@
 // per tile of 128 consecutive rows, with the row tile A densified in shared memory:
 //   - the host lays out the quantised entries per (row tile, 256-column chunk) as 32-bit words
 //     holding the entry's byte offset inside the chunk's operand layout and its e4m3 byte;
+//   - warps are specialised: producer warps stage chunks, one thread issues the MMAs, four
+//     warps read the accumulators, handing over through mbarriers;
 //   - the CTA scatters a chunk's entries into one of two zeroed 32 KB chunk buffers, one thread
 //     issues the chunk's tcgen05.mma (kind::f8f6f4, M = 128, N = 128, K = 32 each) into a
 //     128-column FP32 accumulator in tensor memory, and tcgen05.commit signals an mbarrier when
@@ -31,12 +33,18 @@
 namespace aes {
 namespace dev {
 
-constexpr int kTcThreads = 256;
+// Warp roles: warps 0-7 stage the chunks (producers), warps 8-11 read the accumulators (warp w
+// may only read tensor-memory lanes 32 (w % 4) .. + 31), warp 12 allocates tensor memory and its
+// lane 0 issues the MMAs.  They hand work over through mbarriers only.
+constexpr int kTcProducers = 256;
+constexpr int kTcEpiWarp = 8;
+constexpr int kTcMmaWarp = 12;
+constexpr int kTcThreads = 13 * 32;
 constexpr uint32_t kTcTmemCols = 2 * kTcQ;  // two FP32 accumulators
 
 __host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split) {
   const uint32_t S = split <= 1 ? 1 : split;
-  return tc_qtab_bytes(cols) + 2 * (size_t)kTcChunkBytes + (size_t)S * kTcQ * 4 + 64;
+  return tc_qtab_bytes(cols) + 2 * (size_t)kTcChunkBytes + (size_t)S * kTcQ * 4 + 128;
 }
 
 // e4m3 query operand of queries q0 .. q0 + nq - 1 (zero past nq and past cols)
@@ -51,7 +59,7 @@ __global__ void k_qtable_tc(const int8_t* __restrict__ q8, uint32_t ld8, uint32_
 }
 
 struct TcArgs {
-  const uint32_t* ent;   // per entry: byte offset in its chunk operand | e4m3 value << 16
+  const uint32_t* ent;   // per entry: byte offset in its chunk operand << 16 | e4m3 value
   const uint32_t* ptr;   // [n_rtiles * nch + 1] first entry of (row tile, chunk)
   uint32_t n_rtiles, nch, kpad, n_rows;
   const uint8_t* qt;     // e4m3 query operand of this launch, tc_qtab_bytes(cols)
@@ -75,8 +83,10 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(2048u >> 4) << 16) |
          ((uint64_t)(128u >> 4) << 32) | ((uint64_t)1 << 46);
 }
-// waits for the phase of the given parity to complete; gives up after about a second
-__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+// Waits for the phase of the given parity to complete.  Gives up after about a second, or as
+// soon as another thread of the CTA has given up (*abort set), so that every role leaves its
+// loop instead of waiting on a partner that has left.
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile uint32_t* abort) {
   const long long t0 = clock64();
   uint32_t done = 0;
   while (!done) {
@@ -84,9 +94,17 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-    if (!done && clock64() - t0 > (1ll << 31)) return false;
+    if (done) break;
+    if (*abort) return false;
+    if (clock64() - t0 > (1ll << 31)) {
+      *abort = 1u;
+      return false;
+    }
   }
   return true;
+}
+__device__ __forceinline__ void tc_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -119,16 +137,13 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Reads accumulator `dbuf` of row tile T and appends every (row, query) key at or above the
-// query's threshold.  Warp w holds rows 32 (w % 4) .. + 31 of the tile (its tensor-memory lane
-// quarter) and queries 64 (w / 4) .. + 63.
-__device__ __forceinline__ bool tc_epilogue(const TcArgs& a, uint32_t T, uint32_t tmem,
-                                            uint32_t dbuf, uint32_t bar, uint32_t parity,
-                                            const uint32_t* thr_s, uint32_t S) {
-  const bool ok = tc_wait(bar, parity);
-  tc_fence_after();
+// Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, 128 queries) and
+// appends every (row, query) key at or above the query's threshold.  thf holds the thresholds as
+// FP32 bounds: the score (an exact integer in FP32) or rowscale * score is compared directly.
+__device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_t tmem,
+                                            uint32_t dbuf, const float* thf_all, uint32_t S) {
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t g = warp & 3u, h = warp >> 2;
+  const uint32_t g = warp & 3u;
   const uint32_t row = T * kTcRows + g * 32u + lane;
   const bool valid = row < a.n_rows;
   uint32_t p = 0;
@@ -137,17 +152,16 @@ __device__ __forceinline__ bool tc_epilogue(const TcArgs& a, uint32_t T, uint32_
     p = part_of(row, S, a.slice);
     if (a.rowscale) rs = __ldg(a.rowscale + row);
   }
-  const float* thf = reinterpret_cast<const float*>(thr_s) + p * kTcQ;
+  const float* thf = thf_all + p * kTcQ;
 #pragma unroll 1
-  for (uint32_t cc = 0; cc < 2; cc++) {
-    const uint32_t col0 = h * 64u + cc * 32u;
+  for (uint32_t col0 = 0; col0 < kTcQ; col0 += 32u) {
     uint32_t v[32];
     tc_ld32(tmem + dbuf * kTcQ + col0 + ((g * 32u) << 16), v);
     if (valid) {
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const uint32_t q = col0 + j;
-        const float f = __uint_as_float(v[j]);  // an exact integer score
+        const float f = __uint_as_float(v[j]);
         const float x = a.rowscale ? __fmul_rn(f, rs) : f;
         if (x >= thf[q] && q < a.nq) {
           const uint32_t key = a.rowscale ? key_f32(x) : key_i32(__float2int_rn(f));
@@ -158,13 +172,11 @@ __device__ __forceinline__ bool tc_epilogue(const TcArgs& a, uint32_t T, uint32_
       }
     }
   }
-  tc_fence_before();
-  return ok;
 }
 
-constexpr int kTcPer = 8;  // entries of a chunk a thread holds in registers (2048 per chunk)
+constexpr int kTcPer = 8;  // entries of a chunk a producer thread holds (2048 per chunk)
 
-// A thread's share of one chunk's entries: v[u] = entry b + tid + 256 u for tid + 256 u < n
+// A producer's share of one chunk's entries: v[u] = entry b + tid + 256 u for tid + 256 u < n
 struct TcEnt {
   uint32_t v[kTcPer];
   uint32_t b = 0, n = 0;
@@ -173,7 +185,7 @@ struct TcEnt {
     n = n_;
 #pragma unroll
     for (int u = 0; u < kTcPer; u++) {
-      const uint32_t i = tid + (uint32_t)u * kTcThreads;
+      const uint32_t i = tid + (uint32_t)u * kTcProducers;
       v[u] = i < n ? __ldg(ent + b + i) : 0u;
     }
   }
@@ -182,26 +194,40 @@ struct TcEnt {
                                         bool clear) const {
 #pragma unroll
     for (int u = 0; u < kTcPer; u++) {
-      const uint32_t i = tid + (uint32_t)u * kTcThreads;
-      if (i < n) ab[v[u] & 0xFFFFu] = clear ? (uint8_t)0 : (uint8_t)(v[u] >> 16);
+      const uint32_t i = tid + (uint32_t)u * kTcProducers;
+      if (i < n) ab[v[u] >> 16] = clear ? (uint8_t)0 : (uint8_t)v[u];
     }
-    for (uint32_t i = tid + kTcPer * kTcThreads; i < n; i += kTcThreads) {
+    for (uint32_t i = tid + kTcPer * kTcProducers; i < n; i += kTcProducers) {
       const uint32_t e = __ldg(ent + b + i);
-      ab[e & 0xFFFFu] = clear ? (uint8_t)0 : (uint8_t)(e >> 16);
+      ab[e >> 16] = clear ? (uint8_t)0 : (uint8_t)e;
     }
   }
 };
 
-// One CTA per SM, persistent over row tiles T = blockIdx.x, + gridDim.x, ...
+// OR of `fail` over the producer threads (named barrier 1)
+__device__ __forceinline__ bool tc_producers_any(bool fail) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred f, r;\n setp.ne.u32 f, %1, 0;\n bar.red.or.pred r, 1, %2, f;\n"
+      " selp.u32 %0, 1, 0, r;\n}\n"
+      : "=r"(r) : "r"((uint32_t)fail), "n"(kTcProducers) : "memory");
+  return r != 0;
+}
+
+// One CTA per SM, persistent over row tiles T = blockIdx.x, + gridDim.x, ...  Chunk i of the CTA
+// is chunk i % nch of its tile i / nch; chunk buffer i & 1; accumulator (tile t) t & 1.
 __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t qbytes = (a.kpad / 16u) * 2048u;
   unsigned char* sq = smem;                     // query operand
   unsigned char* sa = smem + qbytes;            // two chunk buffers of the row tile
-  uint32_t* thr_s = reinterpret_cast<uint32_t*>(sa + 2 * kTcChunkBytes);
+  float* thf = reinterpret_cast<float*>(sa + 2 * kTcChunkBytes);
   const uint32_t S = a.split <= 1 ? 1u : a.split;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(thr_s + S * kTcQ);  // 2 chunk, 2 accumulator
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 4);
+  // mbarriers: staged[2] (producers -> MMA), mma_done[2] (MMA -> producers), acc_full[2]
+  // (MMA -> epilogue), acc_empty[2] (epilogue -> MMA)
+  uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * kTcQ);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+  volatile uint32_t* abort = tslot + 1;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   {
     const uint4* src = reinterpret_cast<const uint4*>(a.qt);
@@ -209,8 +235,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     for (uint32_t i = tid; i < qbytes / 16u; i += blockDim.x) dst[i] = src[i];
     uint4* z = reinterpret_cast<uint4*>(sa);
     for (uint32_t i = tid; i < 2 * kTcChunkBytes / 16u; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
-    // thresholds as FP32 bounds on the score (int keys) or on rowscale * score, so that the
-    // comparison needs no conversion: key >= th  <=>  bound <= x for every x the pass produces
+    // thresholds as FP32 bounds on the score (int keys) or on rowscale * score:
+    // key >= th  <=>  x >= bound for every x the pass produces
     for (uint32_t i = tid; i < S * kTcQ; i += blockDim.x) {
       const uint32_t p = i / kTcQ, q = i % kTcQ;
       const uint32_t th = q < a.nq ? a.thr[(size_t)(a.q0 + q) * S + p] : 0xFFFFFFFFu;
@@ -222,15 +248,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
         fb = b > (1 << 24) ? __int_as_float(0x7f800000)
                            : (b < -(1 << 24) ? -__int_as_float(0x7f800000) : __int2float_rn(b));
       }
-      thr_s[i] = __float_as_uint(fb);
+      thf[i] = fb;
     }
   }
   if (tid == 0) {
-    for (int b = 0; b < 4; b++)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(tc_smem_u32(bars + b)));
+    for (int b = 0; b < 8; b++) {
+      const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers : (b >= 6 ? 128u : 1u);  // 4 epilogue warps
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
+    }
+    *abort = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == kTcMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                  :: "r"(tc_smem_u32(tslot)), "n"(kTcTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -240,105 +269,120 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  // instruction descriptor: FP32 accumulator, e4m3 x e4m3, both K-major, N = 128, M = 128
-  const uint32_t idesc = (1u << 4) | ((kTcQ >> 3) << 17) | ((kTcRows >> 4) << 24);
-  const uint32_t bar_chunk = tc_smem_u32(bars), bar_acc = tc_smem_u32(bars + 2);
-  const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
-  const uint32_t ep_chunk = a.nch > 1 ? 1u : 0u;  // the chunk after which the previous tile's
-                                                  // accumulator is read
-  // Entries move through registers: a thread holds entries tid + 256 u (u < kTcPer) of a chunk,
-  // chunk i in ring set E[i % 4].  Step i clears chunk i - 2 from E[(i + 2) % 4], then loads
-  // chunk i + 2 into it, and stages chunk i (loaded two steps earlier); the row offsets of a
-  // chunk are read four steps before its entries.  The ring has static names (the step is
-  // unrolled four times), so no register copy waits on a load in flight.  Chunks of more than
-  // 256 kTcPer entries read the rest from global memory.
+  const uint32_t b_staged = tc_smem_u32(bars), b_done = tc_smem_u32(bars + 2);
+  const uint32_t b_full = tc_smem_u32(bars + 4), b_empty = tc_smem_u32(bars + 6);
   const uint32_t ntl = a.n_rtiles > blockIdx.x ? (a.n_rtiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
   const uint32_t total = ntl * a.nch;  // chunks of this CTA
-  auto chunk_id = [&](uint32_t i) -> uint32_t {
-    return i < total ? (blockIdx.x + (i / a.nch) * gridDim.x) * a.nch + i % a.nch : 0xFFFFFFFFu;
-  };
-  auto ptr_of = [&](uint32_t i, uint32_t& b, uint32_t& e) {
-    const uint32_t j = chunk_id(i);
-    b = j != 0xFFFFFFFFu ? __ldg(a.ptr + j) : 0u;
-    e = j != 0xFFFFFFFFu ? __ldg(a.ptr + j + 1) : 0u;
-  };
-  TcEnt E0, E1, E2, E3;
-  uint32_t P0b, P0e, P1b, P1e, P2b, P2e, P3b, P3e;  // row offsets of chunk i + 2 in P[(i + 2) % 4]
-  {
-    uint32_t b, e;
-    ptr_of(0, b, e);
-    E0.load(a.ent, b, e - b, tid);
-    ptr_of(1, b, e);
-    E1.load(a.ent, b, e - b, tid);
-    ptr_of(2, P2b, P2e);
-    ptr_of(3, P3b, P3e);
-    ptr_of(4, P0b, P0e);
-    ptr_of(5, P1b, P1e);
-  }
-  // ok: every bounded wait of this thread succeeded.  The CTA leaves the loop together (the
-  // barrier's AND) at the first failure, so a stalled tensor pipe costs one wait, not one per chunk.
-  bool ok = true, live = true;
-  auto step = [&](uint32_t i, TcEnt& cur, TcEnt& old, uint32_t& pb, uint32_t& pe) {
-    const uint32_t tl = i / a.nch, c = i % a.nch;
-    const uint32_t buf = i & 1u;
-    unsigned char* ab = sa + buf * kTcChunkBytes;
-    if (i >= 2) {  // the MMAs of chunk i - 2 have read this buffer: clear its entries
-      ok &= tc_wait(bar_chunk + 8u * buf, ((i - 2) >> 1) & 1u);
-      old.stage(ab, a.ent, tid, true);
+  bool ok = true;
+
+  if (warp < kTcProducers / 32) {
+    // ---- producers ----------------------------------------------------------------------------
+    // Chunk i lives in ring set E[i % 4] (static names: the step is dispatched four ways).  Step i
+    // clears chunk i - 2 from E[(i + 2) % 4], loads chunk i + 2 into it and stages chunk i
+    // (loaded two steps earlier); row offsets are read four steps before the entries.  So no
+    // register a store or a copy reads waits on a load in flight.
+    // chunk id of chunk i: tile blockIdx.x + (i / nch) gridDim.x, chunk i % nch; kept
+    // incrementally for the look-ahead chunk (no division per step)
+    uint32_t la_i = 0, la_t = blockIdx.x, la_c = 0;
+    auto ptr_next = [&](uint32_t& b, uint32_t& e) {  // offsets of chunk la_i, then advance it
+      const bool in = la_i < total;
+      const uint32_t j = la_t * a.nch + la_c;
+      b = in ? __ldg(a.ptr + j) : 0u;
+      e = in ? __ldg(a.ptr + j + 1) : 0u;
+      la_i++;
+      if (++la_c == a.nch) {
+        la_c = 0;
+        la_t += gridDim.x;
+      }
+    };
+    TcEnt E0, E1, E2, E3;
+    uint32_t P0b, P0e, P1b, P1e, P2b, P2e, P3b, P3e;  // row offsets of chunk i + 2 in P[(i + 2) % 4]
+    {
+      uint32_t b, e;
+      ptr_next(b, e);
+      E0.load(a.ent, b, e - b, tid);
+      ptr_next(b, e);
+      E1.load(a.ent, b, e - b, tid);
+      ptr_next(P2b, P2e);
+      ptr_next(P3b, P3e);
+      ptr_next(P0b, P0e);
+      ptr_next(P1b, P1e);
     }
-    // every clear lands before any write of this chunk (they may share a byte)
-    if (!__syncthreads_and(ok)) {
-      live = false;
-      return;
+    auto step = [&](uint32_t i, TcEnt& cur, TcEnt& old, uint32_t& pb, uint32_t& pe) -> bool {
+      const uint32_t buf = i & 1u;
+      unsigned char* ab = sa + buf * kTcChunkBytes;
+      if (i >= 2) {  // the MMAs of chunk i - 2 have read this buffer: clear its entries
+        ok &= tc_wait(b_done + 8u * buf, ((i - 2) >> 1) & 1u, abort);
+        if (ok) old.stage(ab, a.ent, tid, true);
+      }
+      // every clear lands before any write of this chunk (they may share a byte); the
+      // producers leave together at the first failure
+      if (tc_producers_any(!ok)) return false;
+      old.load(a.ent, pb, pe - pb, tid);  // chunk i + 2
+      ptr_next(pb, pe);                   // chunk i + 6
+      cur.stage(ab, a.ent, tid, false);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc_arrive(b_staged + 8u * buf);
+      return true;
+    };
+    for (uint32_t i = 0; i < total; i++) {
+      bool go;
+      switch (i & 3u) {
+        case 0: go = step(i, E0, E2, P2b, P2e); break;
+        case 1: go = step(i, E1, E3, P3b, P3e); break;
+        case 2: go = step(i, E2, E0, P0b, P0e); break;
+        default: go = step(i, E3, E1, P1b, P1e); break;
+      }
+      if (!go) break;
     }
-    old.load(a.ent, pb, pe - pb, tid);  // chunk i + 2
-    ptr_of(i + 6, pb, pe);
-    cur.stage(ab, a.ent, tid, false);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
+  } else if (warp < kTcEpiWarp + 4) {
+    // ---- epilogue -----------------------------------------------------------------------------
+    for (uint32_t tl = 0; tl < ntl; tl++) {
+      const uint32_t d = tl & 1u;
+      ok &= tc_wait(b_full + 8u * d, (tl >> 1) & 1u, abort);
+      ok = __all_sync(0xFFFFFFFFu, ok);  // tcgen05.ld needs the whole warp
+      if (!ok) break;
+      tc_fence_after();
+      tc_epilogue(a, blockIdx.x + tl * gridDim.x, tmem, d, thf, S);
+      tc_fence_before();
+      tc_arrive(b_empty + 8u * d);
+    }
+  } else if ((tid & 31u) == 0) {
+    // ---- MMA issue (one thread) ---------------------------------------------------------------
+    // instruction descriptor: FP32 accumulator, e4m3 x e4m3, both K-major, N = 128, M = 128
+    const uint32_t idesc = (1u << 4) | ((kTcQ >> 3) << 17) | ((kTcRows >> 4) << 24);
+    const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
+    uint32_t tl = 0, c = 0;
+    for (uint32_t i = 0; i < total; i++) {
+      const uint32_t buf = i & 1u, d = tl & 1u;
+      if (c == 0 && tl >= 2) ok &= tc_wait(b_empty + 8u * d, ((tl - 2) >> 1) & 1u, abort);
+      if (ok) ok &= tc_wait(b_staged + 8u * buf, (i >> 1) & 1u, abort);
+      if (!ok) break;
       tc_fence_after();
       const uint32_t nk = min(kTcChunkK, a.kpad - c * kTcChunkK) / 32u;
-      const uint32_t d = tmem + (tl & 1u) * kTcQ;
       for (uint32_t kk = 0; kk < nk; kk++)
-        tc_mma(d, tc_desc(sa_addr + buf * kTcChunkBytes + kk * 4096u),
+        tc_mma(tmem + d * kTcQ, tc_desc(sa_addr + buf * kTcChunkBytes + kk * 4096u),
                tc_desc(sq_addr + (c * 16u + 2u * kk) * 2048u), idesc, (c | kk) != 0);
-      tc_commit(bar_chunk + 8u * buf);
-      if (c == a.nch - 1) tc_commit(bar_acc + 8u * (tl & 1u));
+      tc_commit(b_done + 8u * buf);
+      if (c == a.nch - 1) tc_commit(b_full + 8u * d);
+      if (++c == a.nch) {
+        c = 0;
+        tl++;
+      }
     }
-  };
-  for (uint32_t i = 0; i < total; i++) {
-    switch (i & 3u) {  // static ring names: four inlined copies of the step
-      case 0: step(i, E0, E2, P2b, P2e); break;
-      case 1: step(i, E1, E3, P3b, P3e); break;
-      case 2: step(i, E2, E0, P0b, P0e); break;
-      default: step(i, E3, E1, P1b, P1e); break;
-    }
-    if (!live) break;
-    const uint32_t tl = i / a.nch;
-    if (tl > 0 && i % a.nch == ep_chunk)  // the previous tile's accumulator
-      ok &= tc_epilogue(a, blockIdx.x + (tl - 1) * gridDim.x, tmem, (tl - 1) & 1u,
-                        bar_acc + 8u * ((tl - 1) & 1u), ((tl - 1) >> 1) & 1u, thr_s, S);
+    // the last arrivals on the chunk barriers land before the CTA's shared memory goes away
+    if (ok && total >= 1) ok &= tc_wait(b_done + 8u * ((total - 1) & 1u), ((total - 1) >> 1) & 1u, abort);
+    if (ok && total >= 2) ok &= tc_wait(b_done + 8u * ((total - 2) & 1u), ((total - 2) >> 1) & 1u, abort);
   }
-  const uint32_t it = total;
-  if (__syncthreads_and(ok && live) && ntl > 0) {
-    const uint32_t tl = ntl - 1;
-    ok &= tc_epilogue(a, blockIdx.x + tl * gridDim.x, tmem, tl & 1u, bar_acc + 8u * (tl & 1u),
-                      (tl >> 1) & 1u, thr_s, S);
-  }
-  // the chunk barriers' last arrivals land before the CTA (and its shared memory) goes away
-  if (__syncthreads_and(ok && live)) {
-    if (it >= 1) ok &= tc_wait(bar_chunk + 8u * ((it - 1) & 1u), ((it - 1) >> 1) & 1u);
-    if (it >= 2) ok &= tc_wait(bar_chunk + 8u * ((it - 2) & 1u), ((it - 2) >> 1) & 1u);
-  }
+  tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == kTcMmaWarp) {
+    __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "n"(kTcTmemCols));
   }
-  if (!ok) {
-    for (uint32_t q = tid; q < a.nq; q += blockDim.x) atomicOr(a.status + a.q0 + q, ST_DEVICE);
+  if (*abort && tid == 0) {
+    for (uint32_t q = 0; q < a.nq; q++) atomicOr(a.status + a.q0 + q, ST_DEVICE);
   }
 }
 
