@@ -33,13 +33,15 @@
 namespace aes {
 namespace dev {
 
-// Warp roles: warps 0-7 stage the chunks (producers), warps 8-11 read the accumulators (warp w
-// may only read tensor-memory lanes 32 (w % 4) .. + 31), warp 12 allocates tensor memory and its
-// lane 0 issues the MMAs.  They hand work over through mbarriers only.
+// Warp roles: warps 0-7 stage the chunks (producers), warps 8-15 read the accumulators (warp w
+// may only read tensor-memory lanes 32 (w % 4) .. + 31; warps 8-11 take queries 0-63, warps
+// 12-15 queries 64-127), warp 16 allocates tensor memory and its lane 0 issues the MMAs.  They
+// hand work over through mbarriers only.
 constexpr int kTcProducers = 256;
 constexpr int kTcEpiWarp = 8;
-constexpr int kTcMmaWarp = 12;
-constexpr int kTcThreads = 13 * 32;
+constexpr int kTcEpilogue = 256;
+constexpr int kTcMmaWarp = 16;
+constexpr int kTcThreads = 17 * 32;
 constexpr uint32_t kTcTmemCols = 2 * kTcQ;  // two FP32 accumulators
 
 __host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split) {
@@ -137,13 +139,15 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, 128 queries) and
+// Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, 64 queries) and
 // appends every (row, query) key at or above the query's threshold.  thf holds the thresholds as
 // FP32 bounds: the score (an exact integer in FP32) or rowscale * score is compared directly.
+// A block of 32 queries is compared without branches; only a block holding a hit (rare: the
+// thresholds pass about the Top-CK rows) takes the append path.
 __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_t tmem,
                                             uint32_t dbuf, const float* thf_all, uint32_t S) {
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t g = warp & 3u;
+  const uint32_t g = warp & 3u, h = (warp - kTcEpiWarp) >> 2;
   const uint32_t row = T * kTcRows + g * 32u + lane;
   const bool valid = row < a.n_rows;
   uint32_t p = 0;
@@ -154,16 +158,25 @@ __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_
   }
   const float* thf = thf_all + p * kTcQ;
 #pragma unroll 1
-  for (uint32_t col0 = 0; col0 < kTcQ; col0 += 32u) {
+  for (uint32_t col0 = h * 64u; col0 < h * 64u + 64u; col0 += 32u) {
     uint32_t v[32];
     tc_ld32(tmem + dbuf * kTcQ + col0 + ((g * 32u) << 16), v);
-    if (valid) {
+    float t[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) t[j] = thf[col0 + j];
+    bool any = false;
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      const float f = __uint_as_float(v[j]);
+      any |= (a.rowscale ? __fmul_rn(f, rs) : f) >= t[j];
+    }
+    if (valid && any) {
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const uint32_t q = col0 + j;
         const float f = __uint_as_float(v[j]);
         const float x = a.rowscale ? __fmul_rn(f, rs) : f;
-        if (x >= thf[q] && q < a.nq) {
+        if (x >= t[j] && q < a.nq) {
           const uint32_t key = a.rowscale ? key_f32(x) : key_i32(__float2int_rn(f));
           const size_t qp = (size_t)(a.q0 + q) * S + p;
           const uint32_t i = atomicAdd(a.cnt + qp, 1u);
@@ -253,7 +266,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   }
   if (tid == 0) {
     for (int b = 0; b < 8; b++) {
-      const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers : (b >= 6 ? 128u : 1u);  // 4 epilogue warps
+      const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers : (b >= 6 ? (uint32_t)kTcEpilogue : 1u);
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
     }
     *abort = 0u;
@@ -335,7 +348,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
       }
       if (!go) break;
     }
-  } else if (warp < kTcEpiWarp + 4) {
+  } else if (warp < kTcEpiWarp + kTcEpilogue / 32) {
     // ---- epilogue -----------------------------------------------------------------------------
     for (uint32_t tl = 0; tl < ntl; tl++) {
       const uint32_t d = tl & 1u;
