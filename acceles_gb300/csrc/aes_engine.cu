@@ -1074,6 +1074,37 @@ int aes_pack_host(const uint64_t* ptr, const uint32_t* col, const float* val, ui
   return AES_OK;
 }
 
+int aes_pack_tc_host(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                     uint32_t cols, const aes_params* p, uint32_t* tile_ptr, uint64_t cap_ptr,
+                     uint32_t* entries, uint64_t cap_entries, uint64_t* n_ptr,
+                     uint64_t* n_entries) {
+  if (!n_ptr || !n_entries || !ptr) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  int rc = validate_params(p, rows, cols);
+  if (rc) return rc;
+  rc = aes::check_csr(ptr, col, rows, cols);
+  if (rc) return rc;
+  aes::HostCSR m;
+  m.rows = rows;
+  m.cols = cols;
+  m.ptr.assign(ptr, ptr + rows + 1);
+  m.col.assign(col, col + ptr[rows]);
+  m.val.assign(val, val + ptr[rows]);
+  aes::PackedMatrix pm;
+  rc = aes::quantize_and_pack(m, *p, &pm);
+  if (rc) return rc;
+  *n_ptr = pm.tc_ptr.size();
+  *n_entries = pm.tc_ent.size();
+  if (tile_ptr) {
+    if (cap_ptr < pm.tc_ptr.size()) return aes::fail(AES_ERR_INVALID, "tile_ptr buffer too small");
+    std::memcpy(tile_ptr, pm.tc_ptr.data(), pm.tc_ptr.size() * 4);
+  }
+  if (entries) {
+    if (cap_entries < pm.tc_ent.size()) return aes::fail(AES_ERR_INVALID, "entry buffer too small");
+    std::memcpy(entries, pm.tc_ent.data(), pm.tc_ent.size() * 4);
+  }
+  return AES_OK;
+}
+
 int aes_destroy(aes_handle* h) {
   if (!h) return AES_OK;
   delete h;

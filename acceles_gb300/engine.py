@@ -40,7 +40,7 @@ GEN_FIXED_UNIFORM = 3
 
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
            "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
-           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact",
+           "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_pack_tc_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact",
            "aes_retune", "aes_read_mtx", "aes_free", "aes_write_mtx", "aes_resparse"]
 
 FLAG_PROFILE = 1
@@ -140,6 +140,10 @@ def load(build_if_missing: bool = True):
     L.aes_pack_host.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.POINTER(Params), ctypes.c_void_p, ctypes.c_uint64, _u64p,
                                 _u32p]
+    L.aes_pack_tc_host.restype = ctypes.c_int
+    L.aes_pack_tc_host.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                   ctypes.POINTER(Params), _u32p, ctypes.c_uint64, _u32p,
+                                   ctypes.c_uint64, _u64p, _u64p]
     L.aes_run_noalloc.restype = ctypes.c_int
     L.aes_run_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -215,6 +219,26 @@ def pack_host(ptr, col, val, rows, cols, **params):
                            ctypes.byref(prm), pk.ctypes.data_as(ctypes.c_void_p), n.value,
                            ctypes.byref(n), _p(trb, _u32p)))
     return pk[: n.value], trb
+
+
+def pack_tc_host(ptr, col, val, rows, cols, **params):
+    """Host-only tensor-core tile layout of a 4-bit matrix (no device): (tile_ptr u32,
+    entries u32); empty arrays when the layout is not built."""
+    L = load()
+    prm = default_params(**params)
+    ptr = np.ascontiguousarray(ptr, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    val = np.ascontiguousarray(val, np.float32)
+    n_ptr, n_ent = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(L.aes_pack_tc_host(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                              ctypes.byref(prm), None, 0, None, 0, ctypes.byref(n_ptr),
+                              ctypes.byref(n_ent)))
+    tp = np.zeros(max(n_ptr.value, 1), np.uint32)
+    ent = np.zeros(max(n_ent.value, 1), np.uint32)
+    _check(L.aes_pack_tc_host(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                              ctypes.byref(prm), _p(tp, _u32p), n_ptr.value, _p(ent, _u32p),
+                              n_ent.value, ctypes.byref(n_ptr), ctypes.byref(n_ent)))
+    return tp[: n_ptr.value], ent[: n_ent.value]
 
 
 MTX_ZERO_INDEXED = 1

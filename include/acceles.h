@@ -197,6 +197,19 @@ int aes_pack_host(const uint64_t* ptr, const uint32_t* col, const float* val, ui
                   uint32_t cols, const aes_params* p, uint8_t* packets, uint64_t cap_packets,
                   uint64_t* n_packets, uint32_t* tile_rowbase);
 
+/* Host-only: the tensor-core tile layout that aes_create builds for a 4-bit matrix with
+ * AES_FLAG_TENSOR in p->flags (no device needed; no reference counterpart).  Entries of each
+ * 128-row tile grouped by 256-column chunk, tile-major; entry = (byte offset of (row in tile,
+ * column in chunk) in the K-major FP8 operand: (k/16)*2048 + (r/8)*128 + (r%8)*16 + k%16) << 16
+ * | e4m3 byte of the quantised value.  tile_ptr[t * chunks + c] is the first entry of (tile t,
+ * chunk c); chunks = ceil(ceil32(cols) / 256).  Pass NULL arrays to get the sizes only;
+ * *n_entries = 0 when the layout is not built (not 4-bit, flag clear, or a repeated
+ * (row, col)). */
+int aes_pack_tc_host(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                     uint32_t cols, const aes_params* p, uint32_t* tile_ptr, uint64_t cap_ptr,
+                     uint32_t* entries, uint64_t cap_entries, uint64_t* n_ptr,
+                     uint64_t* n_entries);
+
 /* ---- seeded synthetic matrices (the reference matrices are not shipped) ------------------ */
 #define AES_GEN_UNIFORM_DEG 0 /* degree U{p0..p1}, distinct uniform columns, values U(0,1) */
 #define AES_GEN_FIXED_ABSNORMAL 1 /* degree p0, distinct uniform columns, values |N(0,1)| */

@@ -154,3 +154,63 @@ def test_baseline_library_exports_its_header():
     L = G.load()
     for name in decl:
         assert hasattr(L, name), name
+
+
+def _e4m3_value(b):
+    """Value of an FP8 e4m3 byte from the format: sign, 4-bit exponent biased by 7, 3-bit
+    mantissa (normal numbers; subnormals 2^-6 * m/8)."""
+    s = -1.0 if b & 0x80 else 1.0
+    e, m = (b >> 3) & 15, b & 7
+    return s * (2.0 ** (e - 7) * (1 + m / 8) if e else 2.0 ** -6 * m / 8)
+
+
+@pytest.mark.parametrize("quant,cols,rows", [(orc.QUANT_SYM_GLOBAL, 1024, 700),
+                                             (orc.QUANT_UNSIGNED_ROW, 500, 300),
+                                             (orc.QUANT_UNSIGNED_GLOBAL, 200, 257)])
+def test_tensor_tile_layout_decodes_to_quantised_matrix(quant, cols, rows):
+    """Every entry of the tensor-core layout names its (row, column) through the operand offset
+    and holds the quantised value exactly in e4m3; together they are the oracle's quantised
+    matrix, each entry once, in the (tile, chunk) slot its row and column fall in."""
+    ptr, col, val = E.gen_matrix(E.GEN_UNIFORM_DEG, rows, cols, 3, 40, seed=cols)
+    if quant == orc.QUANT_SYM_GLOBAL:
+        val = (val * 2 - 1).astype(np.float32)
+    m = orc.Matrix(rows, cols, ptr, col, val, 4, quant)
+    tp, ent = E.pack_tc_host(ptr, col, val, rows, cols, bits=4, quant=quant, flags=E.FLAG_TENSOR)
+    nch = ((cols + 31) // 32 * 32 + 255) // 256
+    ntile = (rows + 127) // 128
+    assert len(tp) == ntile * nch + 1 and tp[0] == 0 and len(ent) == len(m.qcol) == tp[-1]
+    got = set()
+    for t in range(ntile):
+        for c in range(nch):
+            for e in ent[tp[t * nch + c]:tp[t * nch + c + 1]]:
+                off, b = int(e) >> 16, int(e) & 0xFF
+                assert int(e) & 0xFF00 == 0
+                kk, rem = divmod(off, 2048)
+                rg, rem = divmod(rem, 128)
+                rl, kl = divmod(rem, 16)
+                r, k = rg * 8 + rl, kk * 16 + kl
+                assert r < 128 and k < 256
+                got.add((t * 128 + r, c * 256 + k, _e4m3_value(b)))
+    qv = m.qval.astype(np.int64)
+    want = set()
+    for r in range(rows):
+        for i in range(int(m.qptr[r]), int(m.qptr[r + 1])):
+            want.add((r, int(m.qcol[i]), float(qv[i])))
+    assert got == want and len(want) == len(ent)
+
+
+def test_tensor_tile_layout_only_for_4bit_without_repeats():
+    ptr, col, val = E.gen_matrix(E.GEN_UNIFORM_DEG, 300, 64, 3, 6, seed=2)
+    for bits in (6, 8):
+        tp, ent = E.pack_tc_host(ptr, col, val, 300, 64, bits=bits, quant=1, flags=E.FLAG_TENSOR)
+        assert len(ent) == 0
+    tp, ent = E.pack_tc_host(ptr, col, val, 300, 64, bits=4, quant=1, flags=0)
+    assert len(ent) == 0
+    # row 5 holds its first column twice (sorted CSR with a repeat)
+    p = ptr.astype(np.int64)
+    col2 = np.insert(col, p[5] + 1, col[p[5]])
+    val2 = np.insert(val, p[5] + 1, np.float32(0.5))
+    ptr2 = ptr.copy()
+    ptr2[6:] += 1
+    tp, ent = E.pack_tc_host(ptr2, col2, val2, 300, 64, bits=4, quant=1, flags=E.FLAG_TENSOR)
+    assert len(ent) == 0
