@@ -178,18 +178,37 @@ static void build_tc_layout(const std::vector<uint64_t>& qptr, const std::vector
     if (dup[t]) return;
   out->tc_ptr.assign(nt * nch + 1, 0);
   for (uint64_t j = 0; j < nt * nch; j++) out->tc_ptr[j + 1] = out->tc_ptr[j] + cnt[j];
+  // Within a (tile, chunk) the order is free: entries go round-robin over the 32 shared-memory
+  // banks their bytes fall in (bank = offset / 4 % 32), so the 32 consecutive entries one warp
+  // writes with one store instruction hit distinct banks as long as every bank has entries left.
   out->tc_ent.assign(qnnz, 0);
   parallel_for(nt, 64, [&](uint64_t b, uint64_t e) {
-    std::vector<uint32_t> fill(nch);
+    std::vector<std::vector<uint32_t>> chunk(nch);
+    std::vector<uint32_t> bank_n(32), keyed;
     for (uint64_t t = b; t < e; t++) {
-      for (uint32_t c = 0; c < nch; c++) fill[c] = out->tc_ptr[t * nch + c];
+      for (auto& v : chunk) v.clear();
       const uint64_t r1 = std::min<uint64_t>(rows, (t + 1) * kTcRows);
       for (uint64_t r = t * kTcRows; r < r1; r++) {
         for (uint64_t i = qptr[r]; i < qptr[r + 1]; i++) {
           const uint32_t c = qcol[i] / kTcChunkK, k = qcol[i] % kTcChunkK;
-          out->tc_ent[fill[c]++] = (tc_off((uint32_t)(r - t * kTcRows), k) << 16) |
-                                   (uint32_t)e4m3_small((int)qval[i]);
+          chunk[c].push_back((tc_off((uint32_t)(r - t * kTcRows), k) << 16) |
+                             (uint32_t)e4m3_small((int)qval[i]));
         }
+      }
+      for (uint32_t c = 0; c < nch; c++) {
+        // key = (rank among the entries of its bank) * 32 + bank; ascending keys go round-robin
+        std::fill(bank_n.begin(), bank_n.end(), 0u);
+        keyed.clear();
+        for (size_t j = 0; j < chunk[c].size(); j++) {
+          const uint32_t bank = (chunk[c][j] >> 18) & 31u;
+          keyed.push_back(bank_n[bank]++ * 32u + bank);
+        }
+        std::vector<uint32_t> order(chunk[c].size());
+        for (size_t j = 0; j < order.size(); j++) order[j] = (uint32_t)j;
+        std::sort(order.begin(), order.end(),
+                  [&](uint32_t x, uint32_t y) { return keyed[x] < keyed[y]; });
+        uint32_t* dst = out->tc_ent.data() + out->tc_ptr[t * nch + c];
+        for (size_t j = 0; j < order.size(); j++) dst[j] = chunk[c][order[j]];
       }
     }
   });

@@ -11,17 +11,16 @@
 // per tile of 128 consecutive rows, with the row tile A densified in shared memory:
 //   - the host lays out the quantised entries per (row tile, 256-column chunk) as 32-bit words
 //     holding the entry's byte offset inside the chunk's operand layout and its e4m3 byte;
-//   - warps are specialised: producer warps stage chunks, one thread issues the MMAs, four
-//     warps read the accumulators, handing over through mbarriers;
-//   - the CTA scatters a chunk's entries into one of two zeroed 32 KB chunk buffers, one thread
-//     issues the chunk's tcgen05.mma (kind::f8f6f4, M = 128, N = 128, K = 32 each) into a
-//     128-column FP32 accumulator in tensor memory, and tcgen05.commit signals an mbarrier when
-//     they have read the buffer; the entries are then written back to zero (the buffer is reused
-//     two chunks later);
-//   - after a tile's last chunk the accumulator (one of two) is read with tcgen05.ld while the
-//     next tile's MMAs run: every (row, query) score becomes the same candidate key as in the
-//     other passes and is compared with the query's threshold; hits are appended exactly as
-//     the dp4a pass appends them.
+//   - producer warps write a chunk's entries into one of two zeroed 32 KB chunk buffers (and
+//     write them back to zero once the MMAs of that chunk have read the buffer);
+//   - one thread issues the chunk's tcgen05.mma (kind::f8f6f4, M = 128, N = 128, K = 32 each)
+//     into one of two 128-column FP32 accumulators in tensor memory; tcgen05.commit signals
+//     mbarriers when a chunk buffer is read and when a tile's accumulator is complete;
+//   - epilogue warps read a complete accumulator with tcgen05.ld while the next tile's MMAs run:
+//     every (row, query) score becomes the same candidate key as in the other passes and is
+//     compared with the query's threshold; hits are appended exactly as the dp4a pass appends
+//     them.
+// The roles hand work over through mbarriers only.
 // Both operands are K-major without swizzle (layout in aes_tc_layout.h).
 // Reference counterpart: the candidate pass spmv_ucsr_top_k_multicore.hpp:195-413 (one query per
 // pass on the FPGA); scores equal those of gold_algorithms.hpp:249-308 on the same integers.
@@ -161,9 +160,15 @@ __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_
   for (uint32_t col0 = h * 64u; col0 < h * 64u + 64u; col0 += 32u) {
     uint32_t v[32];
     tc_ld32(tmem + dbuf * kTcQ + col0 + ((g * 32u) << 16), v);
-    float t[32];
+    float t[32];  // the same 32 thresholds for every lane: 16-byte broadcast loads
 #pragma unroll
-    for (int j = 0; j < 32; j++) t[j] = thf[col0 + j];
+    for (int j = 0; j < 8; j++) {
+      const float4 x = reinterpret_cast<const float4*>(thf + col0)[j];
+      t[4 * j] = x.x;
+      t[4 * j + 1] = x.y;
+      t[4 * j + 2] = x.z;
+      t[4 * j + 3] = x.w;
+    }
     bool any = false;
 #pragma unroll
     for (int j = 0; j < 32; j++) {

@@ -191,6 +191,11 @@ def test_tensor_tile_layout_decodes_to_quantised_matrix(quant, cols, rows):
                 r, k = rg * 8 + rl, kk * 16 + kl
                 assert r < 128 and k < 256
                 got.add((t * 128 + r, c * 256 + k, _e4m3_value(b)))
+    # each chunk begins with one entry per bank present: one warp store hits distinct banks
+    for j in range(len(tp) - 1):
+        banks = (ent[tp[j]:tp[j + 1]] >> 18) & 31
+        head = banks[:32]
+        assert len(set(head.tolist())) == min(32, len(set(banks.tolist())))
     qv = m.qval.astype(np.int64)
     want = set()
     for r in range(rows):
