@@ -85,9 +85,9 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
          ((uint64_t)(128u >> 4) << 32) | ((uint64_t)1 << 46);
 }
 // Waits for the phase of the given parity to complete.  Gives up after about a second, or as
-// soon as another thread of the CTA has given up (*abort set), so that every role leaves its
+// soon as another thread of the CTA has given up (*gave_up set), so that every role leaves its
 // loop instead of waiting on a partner that has left.
-__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile uint32_t* abort) {
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile uint32_t* gave_up) {
   const long long t0 = clock64();
   uint32_t done = 0;
   while (!done) {
@@ -96,9 +96,9 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile 
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done) : "r"(bar), "r"(parity) : "memory");
     if (done) break;
-    if (*abort) return false;
+    if (*gave_up) return false;
     if (clock64() - t0 > (1ll << 31)) {
-      *abort = 1u;
+      *gave_up = 1u;
       return false;
     }
   }
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   // (MMA -> epilogue), acc_empty[2] (epilogue -> MMA)
   uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * kTcQ);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
-  volatile uint32_t* abort = tslot + 1;
+  volatile uint32_t* gave_up = tslot + 1;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   {
     const uint4* src = reinterpret_cast<const uint4*>(a.qt);
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
       const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers : (b >= 6 ? (uint32_t)kTcEpilogue : 1u);
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
     }
-    *abort = 0u;
+    *gave_up = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == kTcMmaWarp) {
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
       const uint32_t buf = i & 1u;
       unsigned char* ab = sa + buf * kTcChunkBytes;
       if (i >= 2) {  // the MMAs of chunk i - 2 have read this buffer: clear its entries
-        ok &= tc_wait(b_done + 8u * buf, ((i - 2) >> 1) & 1u, abort);
+        ok &= tc_wait(b_done + 8u * buf, ((i - 2) >> 1) & 1u, gave_up);
         if (ok) old.stage(ab, a.ent, tid, true);
       }
       // every clear lands before any write of this chunk (they may share a byte); the
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     // ---- epilogue -----------------------------------------------------------------------------
     for (uint32_t tl = 0; tl < ntl; tl++) {
       const uint32_t d = tl & 1u;
-      ok &= tc_wait(b_full + 8u * d, (tl >> 1) & 1u, abort);
+      ok &= tc_wait(b_full + 8u * d, (tl >> 1) & 1u, gave_up);
       ok = __all_sync(0xFFFFFFFFu, ok);  // tcgen05.ld needs the whole warp
       if (!ok) break;
       tc_fence_after();
@@ -373,8 +373,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     uint32_t tl = 0, c = 0;
     for (uint32_t i = 0; i < total; i++) {
       const uint32_t buf = i & 1u, d = tl & 1u;
-      if (c == 0 && tl >= 2) ok &= tc_wait(b_empty + 8u * d, ((tl - 2) >> 1) & 1u, abort);
-      if (ok) ok &= tc_wait(b_staged + 8u * buf, (i >> 1) & 1u, abort);
+      if (c == 0 && tl >= 2) ok &= tc_wait(b_empty + 8u * d, ((tl - 2) >> 1) & 1u, gave_up);
+      if (ok) ok &= tc_wait(b_staged + 8u * buf, (i >> 1) & 1u, gave_up);
       if (!ok) break;
       tc_fence_after();
       const uint32_t nk = min(kTcChunkK, a.kpad - c * kTcChunkK) / 32u;
@@ -389,8 +389,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
       }
     }
     // the last arrivals on the chunk barriers land before the CTA's shared memory goes away
-    if (ok && total >= 1) ok &= tc_wait(b_done + 8u * ((total - 1) & 1u), ((total - 1) >> 1) & 1u, abort);
-    if (ok && total >= 2) ok &= tc_wait(b_done + 8u * ((total - 2) & 1u), ((total - 2) >> 1) & 1u, abort);
+    if (ok && total >= 1) ok &= tc_wait(b_done + 8u * ((total - 1) & 1u), ((total - 1) >> 1) & 1u, gave_up);
+    if (ok && total >= 2) ok &= tc_wait(b_done + 8u * ((total - 2) & 1u), ((total - 2) >> 1) & 1u, gave_up);
   }
   tc_fence_before();
   __syncthreads();
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "n"(kTcTmemCols));
   }
-  if (*abort && tid == 0) {
+  if (*gave_up && tid == 0) {
     for (uint32_t q = 0; q < a.nq; q++) atomicOr(a.status + a.q0 + q, ST_DEVICE);
   }
 }
