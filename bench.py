@@ -60,6 +60,64 @@ def profile_traffic(name):
     return int(v) if v is not None else None
 
 
+def tensor_4bit_leg(local, steps=5, warmup=3):
+    """The 4-bit batched sparse-query workload: 20M x 1024, row degree gamma(2, mean 32) capped
+    at 512, per-row unsigned 4-bit, 256 queries of 5-30 % density, K 100, CK 256, split 1.  It
+    runs the batched candidate pass on the tensor cores (FP8 tcgen05 products of 128-row tiles)
+    and, for comparison, with dp4a on the same handle.  Reported: device time of graph-replayed
+    steps, the pass's launch time from profiled steps, and whether two queries' Top-K equals the
+    FP32-only Top-K of the same engine."""
+    from acceles_gb300 import autotune as AT
+    from acceles_gb300 import engine as E
+    rows, cols, nq, k = 20_000_000, 1024, 256, 100
+    ptr, col, val = E.gen_matrix(E.GEN_GAMMA_DEG, rows, cols, 32, 512, seed=4242)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=E.QUANT_UNSIGNED_ROW,
+                 split=1, ck=256, k_max=k, max_batch=nq, batch_tile=128, sample_stride=256,
+                 flags=E.FLAG_GRAPHS | E.FLAG_TENSOR, device=local)
+    del ptr, col, val
+    Q = AT.sparse_queries(2 * nq, cols, 4244)
+    out = {"workload": "20Mx1024 gamma(2, mean 32) cap 512, U(0,1), 4-bit per-row unsigned; "
+                       "256 queries of 5-30 % density; K 100, CK 256, split 1",
+           "tensor_tiles": eng.info()["tensor_tiles"]}
+    for name, tflag in (("tensor_cores", E.FLAG_TENSOR), ("dp4a", 0)):
+        eng.retune(flags=E.FLAG_GRAPHS | tflag)
+        for s in range(warmup):
+            eng.Q_reset(Q[(s % 2) * nq:(s % 2 + 1) * nq])
+            eng(k=k)
+        ns = 0
+        for s in range(steps):
+            eng.Q_reset(Q[(s % 2) * nq:(s % 2 + 1) * nq])
+            ns += eng(k=k)
+        eng.retune(flags=E.FLAG_PROFILE | tflag)
+        eng.Q_reset(Q[:nq])
+        eng(k=k)
+        eng.stats(reset=True)
+        eng(k=k)
+        st = eng.stats(reset=True)
+        out[name] = {"queries_per_s": steps * nq / (ns / 1e9),
+                     "ms_per_step": ns / 1e6 / steps,
+                     "pass_ms_per_128_queries": st["cand_ms"] / max(st["cand_timed"], 1)}
+    # dense FP8 products of one launch: every 128-row tile times the 128-query operand
+    flops = 2.0 * ((rows + 127) // 128) * 128 * 128 * 1024
+    tc = out["tensor_cores"]
+    tc["dense_tflops"] = flops / (tc["pass_ms_per_128_queries"] / 1e3) / 1e12
+    bf16 = 1944.7
+    pk = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        bf16 = float(json.load(open(pk)).get("bf16_tflops", bf16))
+    tc["frac_of_fp8_dense"] = tc["dense_tflops"] / (2 * bf16)
+    tc["fp8_dense_peak_note"] = "FP8 dense taken as twice the measured bf16 TFLOP/s"
+    eng.retune(flags=E.FLAG_TENSOR)
+    eng.Q_reset(Q[:nq])
+    eng(k=k)
+    idx, _ = eng.read_topk()
+    eng.Q_reset(Q[:2])
+    ex, _, _ = eng.run_exact(k=k)
+    out["top_k_identical_to_fp32_only"] = bool(np.array_equal(idx[:2], ex[:2]))
+    eng.close()
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
@@ -264,6 +322,8 @@ def main():
     ap.add_argument("--cpu-queries", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-gpu-baseline", action="store_true")
+    ap.add_argument("--no-tensor", action="store_true",
+                    help="skip the 4-bit tensor-core leg (20M x 1024 sparse-query workload)")
     ap.add_argument("--check", type=int, default=2, help="queries checked against the oracle")
     ap.add_argument("--rows", type=int, default=ROWS, help="smaller matrix, for profiling only")
     ap.add_argument("--workload", default="large", choices=["large", "small"],
@@ -445,6 +505,14 @@ def main():
                  "ms_per_query": ens / 1e6 / 16, "queries_per_s": 16 / (ens / 1e9),
                  "queries_timed": 16}
 
+    # the 4-bit batched sparse-query workload on the tensor cores, beside the dp4a pass
+    tensor4 = None
+    if rank == 0 and not args.no_tensor:
+        try:
+            tensor4 = tensor_4bit_leg(local)
+        except Exception as ex:  # report, do not fail the bench
+            tensor4 = {"unavailable": str(ex)[:200]}
+
     # correctness of the measured configuration (outside the timed regions)
     line_extra = {}
     if rank == 0:
@@ -508,6 +576,7 @@ def main():
             "clocks": clk, "clocks_plain": clk_p,
             "gpu_library_baseline": gpu_lib,
             "gpu_fp32_exact": exact,
+            "tensor_4bit": tensor4,
         }
         line.update(line_extra)
         print(json.dumps(line), flush=True)
