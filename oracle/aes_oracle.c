@@ -1,7 +1,7 @@
 /*
  * aes_oracle.c -- CPU restatement of the AccelES two-stage low-bit Top-K SpMV path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for tests/, smoke() and bench.py's CPU legs.  The
+ * TEST INFRASTRUCTURE ONLY: the oracle of tests/, smoke() and bench.py's CPU legs.  The
  * product library (acceles_gb300) never links or calls this file.
  *
  * Build with -ffp-contract=off: the FP32 gold sums are separately rounded multiply-then-add,

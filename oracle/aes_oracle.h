@@ -1,7 +1,7 @@
 /*
  * aes_oracle.h -- CPU restatement of the AccelES two-stage low-bit Top-K SpMV path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests/, the smoke() entry point and
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: tests/, the smoke() entry point and
  * bench.py's cpu_baseline / reference arm may load it.  The product library never links it and
  * never falls back to it.
  *

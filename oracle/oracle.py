@@ -1,6 +1,6 @@
 """CPU oracle for the two-stage low-bit Top-K SpMV path (TEST INFRASTRUCTURE ONLY).
 
-This module is the checker.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU legs
+This module is the oracle.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU legs
 import it; the product package ``acceles_gb300`` never does.  It wraps ``aes_oracle.c`` (a plain
 C restatement of the reference path, built into ``oracle/_build/liboracle.so``) and, when it was
 compiled on this machine, ``oracle/_ref/libaes_ref.so`` (the reference's own gold code from
