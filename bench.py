@@ -13,10 +13,16 @@ and outputs resident in HBM; `e2e` is the same through the host-buffer C ABI cal
 pass streams from HBM.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Every timed leg runs exactly K steps after W warm-up steps.  The reference arm
+(--impl reference) is the reference's CPU method (the oracle port of its gold code) on all host
+threads; it builds its own copy of the same seeded matrix through the oracle, so the engine
+library is never loaded in that process.
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import re
@@ -54,8 +60,37 @@ def profile_number(name, key):
     return float(m.group(1)) if m else None
 
 
+# kernel sources each committed ncu summary was captured from: a summary whose recorded digest
+# differs from the current sources describes an earlier build, and its figures are not reported
+PROFILE_SOURCES = {
+    "cand_batch_10Mx1024_b8.md": ("aes_batch.cuh", "aes_kernels.cuh"),
+    "cand_pass_10Mx1024_b8.md": ("aes_kernels.cuh",),
+    "cand_tc_2Mx1024_b4.md": ("aes_tc.cuh", "aes_tc_layout.h", "aes_kernels.cuh"),
+}
+
+
+def source_digest(files):
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(REPO, "acceles_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def profile_current(name):
+    """True when the summary records the digest of the kernel sources built now."""
+    p = os.path.join(REPO, "profiles", name)
+    if not os.path.exists(p) or name not in PROFILE_SOURCES:
+        return False
+    m = re.search(r"source_digest:\s*([0-9a-f]{16})", open(p).read())
+    return bool(m) and m.group(1) == source_digest(PROFILE_SOURCES[name])
+
+
 def profile_traffic(name):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if it was
+    captured from the current kernel sources."""
+    if not profile_current(name):
+        return None
     v = profile_number(name, "traffic_bytes_per_launch")
     return int(v) if v is not None else None
 
@@ -168,7 +203,12 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def make_matrix(rows=ROWS):
+def make_matrix(rows=ROWS, oracle_side=False):
+    """The seeded 10M x 1024 matrix; oracle_side builds it through the oracle's restatement of
+    the same generator (identical arrays), so that the engine library stays unloaded."""
+    if oracle_side:
+        import oracle as orc
+        return orc.gen_matrix(orc.GEN_UNIFORM_DEG, rows, COLS, DEG_LO, DEG_HI, seed=SEED)
     from acceles_gb300 import engine as E
     return E.gen_matrix(E.GEN_UNIFORM_DEG, rows, COLS, DEG_LO, DEG_HI, seed=SEED)
 
@@ -177,12 +217,21 @@ def make_queries(n, seed=SEED + 1):
     return np.random.default_rng(seed).random((n, COLS)).astype(np.float32)
 
 
-def cpu_baseline(ptr, col, val, queries, seconds, threads, legs=True):
+def headline_config(rows, nnz, split, batch):
+    """The workload both arms report: identical dicts, so the two lines compare directly."""
+    size = f"{rows // 1_000_000}M" if rows >= 1_000_000 else f"{rows // 1000}k"
+    return {"workload": f"{size}x1024 deg U{{10..30}} U(0,1), 8-bit Ultra-CSR, "
+                        f"CK=1024, K=100, split={split}",
+            "rows": rows, "cols": COLS, "nnz": int(nnz), "bits": BITS, "ck": CK,
+            "split": split, "k": K, "batch": batch,
+            "l2": "inputs larger than L2 (492 MB packets per pass)"}
+
+
+def cpu_baseline(m, queries, seconds, threads, legs=True):
     """The reference's CPU method (oracle port) on this host: the two-stage method on all
     threads (the reported baseline) and, when `legs`, the two-stage method on one thread and
     the FP32 full Top-K on one and on all threads, each a bounded sample."""
     import oracle as orc
-    m = orc.Matrix(len(ptr) - 1, COLS, ptr, col, val, BITS, orc.QUANT_SYM_GLOBAL)
     el, done, _ = orc.bench_two_stage(m, queries, CK, K, nthreads=threads, max_seconds=seconds)
     cb = {"value": done / el, "unit": "queries/s", "cores": threads, "kind": "port",
           "sample": f"{done} queries of the same 10M x 1024 workload: two-stage method "
@@ -200,28 +249,66 @@ def cpu_baseline(ptr, col, val, queries, seconds, threads, legs=True):
             "note": "FP32 full Top-K = spmv_coo_gold_top_k (gold_algorithms.hpp:189-247) "
                     "restated; threads = one row block per host thread, merged",
         }
-    return m, cb
+    return cb
 
 
 def run_reference(args, rank, world):
     """The reference's CPU implementation of the path (the oracle port of its gold code; the
-    reference sources are not on the GPU host), all host threads, same workload and metric."""
+    reference sources are not on the GPU host) on all host threads, same workload, metric and
+    config as the GPU arm.  W warm-up steps, then K timed steps; a step is a bounded sample of
+    the workload (--cpu-step-queries queries).  Only the oracle library is loaded."""
     if rank != 0:
         return
+    import oracle as orc
     threads = os.cpu_count() or 1
-    ptr, col, val = make_matrix()
-    Q = make_queries(max(64, args.cpu_queries))
-    _, cb = cpu_baseline(ptr, col, val, Q, args.cpu_seconds, threads, legs=False)
-    line = {"metric": METRIC, "value": cb["value"], "unit": "queries/s", "impl": "reference",
+    rows = args.rows
+    ptr, col, val = make_matrix(rows, oracle_side=True)
+    m = orc.Matrix(rows, COLS, ptr, col, val, BITS, orc.QUANT_SYM_GLOBAL)
+    per = max(1, args.cpu_step_queries)
+    Q = make_queries(per * (args.warmup + args.steps))
+    for s in range(args.warmup):
+        orc.bench_two_stage(m, Q[s * per:(s + 1) * per], CK, K, nthreads=threads, max_seconds=1e9)
+    total, done = 0.0, 0
+    for s in range(args.warmup, args.warmup + args.steps):
+        el, d, _ = orc.bench_two_stage(m, Q[s * per:(s + 1) * per], CK, K, nthreads=threads,
+                                       max_seconds=1e9)
+        total += el
+        done += d
+    qps = done / total
+    cb = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+          "sample": f"{args.steps} steps of {per} queries of the same workload: two-stage "
+                    f"method (streaming Top-{CK} per row block as gold_algorithms.hpp:249-308, "
+                    f"merge, FP32 rescoring, sort_tuples), {threads} threads, {total:.1f} s"}
+    line = {"metric": METRIC, "value": qps, "unit": "queries/s", "impl": "reference",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded; reference matrices not shipped)",
-            "config": {"workload": "10Mx1024 deg U{10..30} U(0,1), 8-bit Ultra-CSR, CK=1024, K=100, split=1",
-                       "rows": ROWS, "cols": COLS, "bits": BITS, "ck": CK, "k": K},
+            "config": headline_config(rows, ptr[-1], args.split, args.batch_batched),
             "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def check_vs_oracle(m, Q, idx, score, split, nthreads):
+    """Every given query against the oracle (bit-exact rows and FP32 scores) and against float64:
+    recall@K of the float64 Top-K and the largest relative error of a returned FP32 score."""
+    import oracle as orc
+    oi, os_, on = orc.two_stage_many(m, Q, split, CK, K, nthreads=nthreads)
+    exact = True
+    for i in range(Q.shape[0]):
+        n = int(on[i])
+        exact &= bool(np.array_equal(idx[i, :n], oi[i, :n])) and \
+            bool(np.array_equal(score[i, :n], os_[i, :n]))
+    fi, _ = orc.topk_f64_many(m.ptr, m.col, m.val, m.rows, COLS, Q, K, nthreads=nthreads)
+    recall = min(len(set(fi[i].tolist()) & set(idx[i].tolist())) / K for i in range(Q.shape[0]))
+    f64 = orc.rows_f64(m.ptr, m.col, m.val, COLS, Q, idx)
+    ok = np.isfinite(f64) & (f64 != 0)
+    rel = np.abs(score.astype(np.float64)[ok] - f64[ok]) / np.abs(f64[ok])
+    return {"queries": int(Q.shape[0]), "bit_exact_vs_oracle": exact,
+            "recall_at_100_vs_fp64_min": recall,
+            "max_rel_err_vs_fp64": float(rel.max()) if rel.size else 0.0}
 
 
 SMALL_METRIC = "Top-100 queries/s, 400k×500 |N(0,1)| 69 nnz/row, 6-bit, SPLIT=32, CK=512 (plain method, small)"
@@ -312,19 +399,22 @@ def run_small(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=20, help="timed steps of every leg")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=64, help="queries per plain step")
-    ap.add_argument("--batch-batched", type=int, default=256, help="queries per batched step")
-    ap.add_argument("--steps-batched", type=int, default=10)
+    ap.add_argument("--batch-batched", type=int, default=4096,
+                    help="queries per batched step (the headline)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--cpu-queries", type=int, default=512)
+    ap.add_argument("--cpu-step-queries", type=int, default=16,
+                    help="queries per step of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-gpu-baseline", action="store_true")
     ap.add_argument("--no-tensor", action="store_true",
                     help="skip the 4-bit tensor-core leg (20M x 1024 sparse-query workload)")
-    ap.add_argument("--check", type=int, default=2, help="queries checked against the oracle")
+    ap.add_argument("--check", type=int, default=256,
+                    help="queries of one batched step checked against the oracle (spread over "
+                         "the step); every query of one plain step is checked as well")
     ap.add_argument("--rows", type=int, default=ROWS, help="smaller matrix, for profiling only")
     ap.add_argument("--workload", default="large", choices=["large", "small"],
                     help="large: 10M x 1024 (the headline); small: the 400k x 500 plain-method case")
@@ -332,8 +422,8 @@ def main():
                     help="row partitions with a Top-(CK/split) each (the reference default is 32)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.steps = max(1, args.steps)
 
-    args.steps_batched = max(1, args.steps_batched)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -358,9 +448,11 @@ def main():
     ptr, col, val = make_matrix(rows)
     stream = torch.cuda.Stream()  # the engine's kernels and the timing events share it
     sptr = stream.cuda_stream
+    threads = os.cpu_count() or 1
 
-    def measure(eng, B, steps, warmup, tag):
-        """Device-timed steps of B resident queries; returns (ms, stats, repaired, clocks)."""
+    def measure(eng, B, steps, warmup):
+        """Device-timed steps of B resident queries; returns (ms, stats, repaired, clocks, pool,
+        outputs of one more step on the first B queries of the pool)."""
         npool = B * 4
         Qh = make_queries(npool, seed=SEED + 1 + rank)
         dq = torch.from_numpy(Qh).cuda()
@@ -400,7 +492,12 @@ def main():
             t = torch.tensor([ms], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
-        return ms, st, repaired, clk, Qh
+        # one more step on pool slice 0, kept for the oracle check (outside the timed region)
+        step(0)
+        torch.cuda.synchronize()
+        repaired += eng.finish()
+        out = (di.cpu().numpy().view(np.uint32).copy(), ds.cpu().numpy().copy())
+        return ms, st, repaired, clk, Qh, out
 
     # The timed steps replay each shape's launches as a CUDA graph (the serving configuration).
     # Per-launch kernel times for the roofline come from a few more steps afterwards with the
@@ -425,38 +522,40 @@ def main():
         eng.finish()
         sp = eng.stats(reset=True)
         eng.retune(flags=E.FLAG_GRAPHS)
-        return sp["cand_ms"] / max(sp["cand_timed"], 1)
+        return sp["cand_ms"] / max(sp["cand_timed"], 1), sp["cand_launches"] / max(n, 1)
 
     # plain: one candidate pass per query
     Bp = args.batch
     eng_p = E.SpMV(rows, COLS, ptr=ptr, col=col, val=val, max_batch=Bp, batch_tile=1, **common)
     info = eng_p.info()
-    ms_p, st_p, rep_p, clk_p, _ = measure(eng_p, Bp, args.steps, args.warmup, "plain")
+    ms_p, st_p, rep_p, clk_p, Qp_pool, out_p = measure(eng_p, Bp, args.steps, args.warmup)
     plain_qps = world * args.steps * Bp / (ms_p / 1e3)
-    plain_launch_ms = cand_launch_ms(eng_p, Bp)
+    plain_launch_ms, _ = cand_launch_ms(eng_p, Bp)
     eng_p.close()
     # batched: one candidate pass per 128 queries
     Bb = args.batch_batched
     eng = E.SpMV(rows, COLS, ptr=ptr, col=col, val=val, max_batch=Bb, batch_tile=128, **common)
-    ms, st, repaired, clk, Qh = measure(eng, Bb, args.steps_batched, args.warmup, "batched")
+    ms, st, repaired, clk, Qh, out_b = measure(eng, Bb, args.steps, args.warmup)
     B = Bb
-    qps = world * args.steps_batched * Bb / (ms / 1e3)
-    batch_launch_ms = cand_launch_ms(eng, Bb)
+    qps = world * args.steps * Bb / (ms / 1e3)
+    batch_launch_ms, cand_per_step = cand_launch_ms(eng, Bb)
+    blocks = (Bb + 127) // 128
 
-    # dominant kernel of the batched path: the batched candidate pass; algorithmic bytes per
-    # launch = Ultra-CSR packets + tile row bases + the 128-query table
+    # dominant kernel of the batched path: the batched candidate pass; algorithmic bytes of one
+    # 128-query block = Ultra-CSR packets + tile row bases + the block's query table
     alg_bytes = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS * 128
-    cand_ms = batch_launch_ms
+    cand_ms = batch_launch_ms * cand_per_step / blocks  # device time per 128-query block
     achieved = alg_bytes / (cand_ms / 1e3) / 1e9
     plain_alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS
     plain_achieved = plain_alg / (plain_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = profile_traffic("cand_batch_10Mx1024_b8.md")
     # the batched pass is bound by instruction issue, not HBM: warp instructions per group of
-    # four entries (ncu instruction count of the capture) x the groups of one launch, over the
-    # live launch time at the sampled SM clock; an SM issues at most 4 warp instructions a cycle
+    # four entries (ncu instruction count of the capture) x the groups of one block, over the
+    # live time per block at the sampled SM clock; an SM issues at most 4 warp instructions a cycle
     issue = None
-    ipg = profile_number("cand_batch_10Mx1024_b8.md", "warp_instructions_per_group")
+    ipg = (profile_number("cand_batch_10Mx1024_b8.md", "warp_instructions_per_group")
+           if profile_current("cand_batch_10Mx1024_b8.md") else None)
     if ipg:
         groups = info["tiles"] * 32 * (511 // (BITS + 11)) // 4
         sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -465,23 +564,22 @@ def main():
             ipl = ipg * groups
             ach = ipl / (cand_ms / 1e3 * mhz * 1e6 * sms)
             issue = {"bound": "issue", "unit": "warp instructions per SM cycle", "achieved": ach,
-                     "peak": 4.0, "frac": ach / 4.0, "instructions_per_launch": ipl,
-                     "instructions_per_group": ipg, "groups_per_launch": groups,
+                     "peak": 4.0, "frac": ach / 4.0, "instructions_per_block": ipl,
+                     "instructions_per_group": ipg, "groups_per_block": groups,
                      "sm_mhz": mhz, "sms": sms}
     plain_traffic = profile_traffic("cand_pass_10Mx1024_b8.md")
 
-    # end to end through the host-buffer C ABI (batched engine)
-    Kk = max(3, min(args.steps_batched, 10))
+    # end to end through the host-buffer C ABI (batched engine), same K steps
     eng.Q_reset(Qh[:B])
     eng(k=K)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for s in range(Kk):
+    for s in range(args.steps):
         b = (s % 4) * B
         eng.Q_reset(Qh[b:b + B])
         eng(k=K)
     e2e_s = time.perf_counter() - t0
-    e2e_qps = world * Kk * B / e2e_s
+    e2e_qps = world * args.steps * B / e2e_s
 
     # library-SpMV comparison arm on the same matrix and queries (cuSPARSE SpMV + full sort,
     # the reference's GPU baseline method), device time per query
@@ -504,6 +602,7 @@ def main():
         exact = {"method": "FP32 score of every row (column-order sums) + Top-K select",
                  "ms_per_query": ens / 1e6 / 16, "queries_per_s": 16 / (ens / 1e9),
                  "queries_timed": 16}
+    eng.close()
 
     # the 4-bit batched sparse-query workload on the tensor cores, beside the dp4a pass
     tensor4 = None
@@ -513,58 +612,57 @@ def main():
         except Exception as ex:  # report, do not fail the bench
             tensor4 = {"unavailable": str(ex)[:200]}
 
-    # correctness of the measured configuration (outside the timed regions)
+    # correctness of the measured configuration (outside the timed regions): every query of one
+    # plain step and a spread of one batched step against the oracle, and against float64
     line_extra = {}
     if rank == 0:
         import oracle as orc
-        m, cb = (None, None)
+        m = orc.Matrix(rows, COLS, ptr, col, val, BITS, orc.QUANT_SYM_GLOBAL)
+        parity = {}
+        if args.check > 0:
+            sel = np.unique(np.linspace(0, B - 1, min(args.check, B)).astype(np.int64))
+            parity["batched"] = check_vs_oracle(m, Qh[sel], out_b[0][sel], out_b[1][sel],
+                                                args.split, threads)
+            parity["plain"] = check_vs_oracle(m, Qp_pool[:Bp], out_p[0], out_p[1], args.split,
+                                              threads)
+            if exact is not None:
+                allrows = np.arange(rows, dtype=np.uint32)
+                s0 = orc.rescore_f32(m.ptr, m.col, m.val, Qh[0], allrows)
+                xi, xs = orc.sort_tuples_f32(allrows, s0)
+                exact["bit_exact_vs_oracle"] = bool(np.array_equal(ei[0], xi[:K])) and \
+                    bool(np.array_equal(es[0], xs[:K]))
+        line_extra = {"parity": parity,
+                      "parity_checked_queries": sum(v["queries"] for v in parity.values()),
+                      "bit_exact_vs_oracle": all(v["bit_exact_vs_oracle"] for v in parity.values())
+                      if parity else None,
+                      "recall_at_100_vs_fp64": min(v["recall_at_100_vs_fp64_min"]
+                                                   for v in parity.values()) if parity else None,
+                      "max_rel_err_vs_fp64": max(v["max_rel_err_vs_fp64"]
+                                                 for v in parity.values()) if parity else None}
         if not args.no_cpu and world == 1:
-            m, cb = cpu_baseline(ptr, col, val, Qh, args.cpu_seconds, os.cpu_count() or 1)
-        if m is None and args.check > 0:
-            m = orc.Matrix(rows, COLS, ptr, col, val, BITS, orc.QUANT_SYM_GLOBAL)
-        eng.Q_reset(Qh[:B])
-        eng(k=K)
-        ri, rs = eng.read_topk()
-        recalls, exact_ok = [], True
-        for i in range(min(args.check, B)):
-            oi, os_, _ = m.two_stage(Qh[i], args.split, CK, K)
-            exact_ok &= bool(np.array_equal(ri[i], oi)) and bool(np.array_equal(rs[i], os_))
-            f64 = orc.scores_f64(m.ptr, m.col, m.val, Qh[i], rows)
-            top = np.argsort(-f64, kind="stable")[:K]
-            recalls.append(len(set(top.tolist()) & set(ri[i].tolist())) / K)
-        if exact is not None and args.check > 0:
-            allrows = np.arange(rows, dtype=np.uint32)
-            s0 = orc.rescore_f32(m.ptr, m.col, m.val, Qh[0], allrows)
-            xi, xs = orc.sort_tuples_f32(allrows, s0)
-            exact["bit_exact_vs_oracle"] = bool(np.array_equal(ei[0], xi[:K])) and \
-                bool(np.array_equal(es[0], xs[:K]))
-        line_extra = {"parity_checked_queries": min(args.check, B), "bit_exact_vs_oracle": exact_ok,
-                      "recall_at_100_vs_fp64": min(recalls) if recalls else None}
-        if cb:
-            line_extra["cpu_baseline"] = cb
+            Qc = make_queries(max(64, 512), seed=SEED + 5)
+            line_extra["cpu_baseline"] = cpu_baseline(m, Qc, args.cpu_seconds, threads)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
-            "steps": args.steps_batched, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps_batched,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded; reference matrices not shipped)",
-            "config": {"workload": f"{rows // 1_000_000}Mx1024 deg U{{10..30}} U(0,1), 8-bit Ultra-CSR, CK=1024, K=100, split={args.split}",
-                       "rows": rows, "cols": COLS, "nnz": info["nnz"], "bits": BITS, "ck": CK,
-                       "split": args.split,
-                       "k": K, "batch": Bb, "path": "batched (one candidate pass per 128 queries)",
-                       "plain_batch": Bp, "plain_steps": args.steps,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (492 MB packets per pass)"},
+            "config": headline_config(rows, info["nnz"], args.split, Bb),
+            "path": "batched (one candidate pass per 128 queries)",
+            "plain_leg": {"batch": Bp, "steps": args.steps, "ms_per_step": ms_p / args.steps},
+            "parallelism": f"replicas x{world}",
             "batched_qps": qps, "plain_qps": plain_qps, "batched_over_plain": qps / plain_qps,
             "hbm_gbs_batched_pass": achieved, "hbm_gbs_plain_pass": plain_achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_cand_batch<8,signed,FILTER> (128 queries per pass)",
+                         "kernel": "k_cand_batch<8,signed,FILTER> (128 queries per matrix read)",
                          "limiter": "CUDA-core integer issue (gathers, byte transposes, dp4a); "
                                     "one matrix read serves 128 queries",
-                         "alg_bytes_per_launch": alg_bytes, "launch_ms": cand_ms,
+                         "alg_bytes_per_block": alg_bytes, "ms_per_block": cand_ms,
+                         "launches_per_step": cand_per_step, "blocks_per_step": blocks,
                          "issue": issue},
             "plain_roofline": {"bound": "hbm", "achieved": plain_achieved, "peak": peak,
                                "unit": "GB/s", "frac": plain_achieved / peak,

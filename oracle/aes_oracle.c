@@ -702,3 +702,333 @@ uint64_t orc_resparse(const uint64_t* ptr, const uint32_t* col, const float* val
   }
   return o;
 }
+
+/* ---------------------------------------------------------------------------------------- */
+/* Seeded synthetic matrices: the same generator as the engine's aes_gen_matrix (it defines   */
+/* the benchmark workloads; the reference ships no matrices).  Restated here so that the CPU  */
+/* baseline builds its inputs without loading the engine library.                             */
+/* ---------------------------------------------------------------------------------------- */
+
+typedef struct { uint64_t s[4]; } orc_xo_t;
+
+static void orc_xo_seed(orc_xo_t* g, uint64_t seed) {
+  uint64_t x = seed;
+  for (int i = 0; i < 4; i++) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    g->s[i] = z ^ (z >> 31);
+  }
+}
+static inline uint64_t orc_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+static uint64_t orc_xo_next(orc_xo_t* g) {
+  uint64_t* s = g->s;
+  uint64_t r = orc_rotl(s[1] * 5, 7) * 9;
+  uint64_t t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = orc_rotl(s[3], 45);
+  return r;
+}
+static double orc_xo_uniform(orc_xo_t* g) { return (double)(orc_xo_next(g) >> 11) * (1.0 / 9007199254740992.0); }
+static uint32_t orc_xo_below(orc_xo_t* g, uint32_t n) {
+  return (uint32_t)(((orc_xo_next(g) >> 32) * (uint64_t)n) >> 32);
+}
+static uint64_t orc_row_seed(uint64_t seed, uint64_t row, uint64_t stream) {
+  uint64_t z = seed * 0xD1B54A32D192ED03ull + row * 0x9E3779B97F4A7C15ull + stream * 0xA0761D6478BD642Full;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static uint32_t orc_gen_degree(uint32_t kind, uint32_t cols, double p0, double p1, orc_xo_t* g) {
+  uint32_t d = 0;
+  switch (kind) {
+    case ORC_GEN_UNIFORM_DEG: {
+      uint32_t lo = (uint32_t)p0, hi = (uint32_t)p1;
+      d = lo + orc_xo_below(g, hi - lo + 1);
+      break;
+    }
+    case ORC_GEN_FIXED_ABSNORMAL:
+    case ORC_GEN_FIXED_UNIFORM:
+      d = (uint32_t)p0;
+      break;
+    case ORC_GEN_GAMMA_DEG: {
+      double u1 = 1.0 - orc_xo_uniform(g), u2 = 1.0 - orc_xo_uniform(g);
+      double x = -(p0 / 2.0) * log(u1 * u2);
+      double r = nearbyint(x);
+      if (r < 1.0) r = 1.0;
+      if (r > p1) r = p1;
+      d = (uint32_t)r;
+      break;
+    }
+  }
+  return d < cols ? d : cols;
+}
+
+typedef struct {
+  uint32_t kind, cols, r0, r1;
+  double p0, p1;
+  uint64_t seed;
+  const uint64_t* ptr;
+  uint32_t* col;
+  float* val;
+  uint32_t* deg;
+} orc_genjob_t;
+
+static void* orc_gen_deg_run(void* arg) {
+  orc_genjob_t* j = (orc_genjob_t*)arg;
+  for (uint32_t r = j->r0; r < j->r1; r++) {
+    orc_xo_t g;
+    orc_xo_seed(&g, orc_row_seed(j->seed, r, 0));
+    j->deg[r] = orc_gen_degree(j->kind, j->cols, j->p0, j->p1, &g);
+  }
+  return NULL;
+}
+
+static void* orc_gen_row_run(void* arg) {
+  orc_genjob_t* j = (orc_genjob_t*)arg;
+  const uint32_t cols = j->cols, nw = (cols + 63) / 64;
+  uint64_t* bm = (uint64_t*)malloc(sizeof(uint64_t) * nw);
+  for (uint32_t r = j->r0; r < j->r1; r++) {
+    orc_xo_t g;
+    orc_xo_seed(&g, orc_row_seed(j->seed, r, 1));
+    const uint32_t d = (uint32_t)(j->ptr[r + 1] - j->ptr[r]);
+    memset(bm, 0, sizeof(uint64_t) * nw);
+    if (d * 2 <= cols) {
+      uint32_t got = 0;
+      while (got < d) {
+        uint32_t c = orc_xo_below(&g, cols);
+        uint64_t bit = 1ull << (c & 63);
+        if (!(bm[c >> 6] & bit)) { bm[c >> 6] |= bit; got++; }
+      }
+    } else { /* dense rows: the columns to leave out are drawn */
+      for (uint32_t w = 0; w < nw; w++) bm[w] = ~0ull;
+      if (cols & 63) bm[nw - 1] = (1ull << (cols & 63)) - 1;
+      uint32_t drop = cols - d, got = 0;
+      while (got < drop) {
+        uint32_t c = orc_xo_below(&g, cols);
+        uint64_t bit = 1ull << (c & 63);
+        if (bm[c >> 6] & bit) { bm[c >> 6] &= ~bit; got++; }
+      }
+    }
+    uint64_t o = j->ptr[r];
+    for (uint32_t w = 0; w < nw; w++) {
+      uint64_t x = bm[w];
+      while (x) {
+        int b = __builtin_ctzll(x);
+        x &= x - 1;
+        j->col[o++] = w * 64 + (uint32_t)b;
+      }
+    }
+    for (uint64_t k = j->ptr[r]; k < o; k++) {
+      float v;
+      if (j->kind == ORC_GEN_FIXED_ABSNORMAL) {
+        double u1 = 1.0 - orc_xo_uniform(&g), u2 = orc_xo_uniform(&g);
+        v = (float)fabs(sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+      } else {
+        v = (float)orc_xo_uniform(&g);
+      }
+      j->val[k] = v;
+    }
+  }
+  free(bm);
+  return NULL;
+}
+
+static void orc_gen_pass(orc_genjob_t* base, uint32_t rows, int nthreads, void* (*fn)(void*)) {
+  if (nthreads < 1) nthreads = 1;
+  orc_genjob_t* jobs = (orc_genjob_t*)malloc(sizeof(orc_genjob_t) * nthreads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t] = *base;
+    jobs[t].r0 = (uint32_t)((uint64_t)rows * t / nthreads);
+    jobs[t].r1 = (uint32_t)((uint64_t)rows * (t + 1) / nthreads);
+    if (nthreads == 1) fn(&jobs[t]);
+    else pthread_create(&th[t], NULL, fn, &jobs[t]);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+}
+
+uint64_t orc_gen_matrix(uint32_t kind, uint32_t rows, uint32_t cols, double p0, double p1,
+                        uint64_t seed, int nthreads, uint64_t* ptr, uint32_t* col, float* val) {
+  if (kind > ORC_GEN_FIXED_UNIFORM || cols == 0 || rows == 0) return UINT64_MAX;
+  if (kind == ORC_GEN_UNIFORM_DEG && (p1 < p0 || p0 < 0)) return UINT64_MAX;
+  uint32_t* deg = (uint32_t*)malloc(sizeof(uint32_t) * rows);
+  orc_genjob_t base;
+  memset(&base, 0, sizeof(base));
+  base.kind = kind; base.cols = cols; base.p0 = p0; base.p1 = p1; base.seed = seed;
+  base.deg = deg;
+  orc_gen_pass(&base, rows, nthreads, orc_gen_deg_run);
+  uint64_t total = 0;
+  for (uint32_t r = 0; r < rows; r++) total += deg[r];
+  if (!ptr) { free(deg); return total; }
+  ptr[0] = 0;
+  for (uint32_t r = 0; r < rows; r++) ptr[r + 1] = ptr[r] + deg[r];
+  free(deg);
+  base.ptr = ptr; base.col = col; base.val = val;
+  orc_gen_pass(&base, rows, nthreads, orc_gen_row_run);
+  return total;
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* Checks at full size, threaded                                                             */
+/* ---------------------------------------------------------------------------------------- */
+
+typedef struct {
+  const uint64_t *ptr, *qptr;
+  const uint32_t *col, *qcol;
+  const float *val, *rowscale, *queries;
+  const int32_t* qval;
+  uint32_t rows, cols, split, ck, k, q0, q1;
+  int bits, quant, qq;
+  uint32_t *out_idx, *out_n;
+  float* out_score;
+} orc_tsjob_t;
+
+static void* orc_ts_run(void* arg) {
+  orc_tsjob_t* j = (orc_tsjob_t*)arg;
+  uint32_t* cand = (uint32_t*)malloc(sizeof(uint32_t) * (j->ck ? j->ck : 1));
+  for (uint32_t q = j->q0; q < j->q1; q++) {
+    uint32_t cn = 0;
+    j->out_n[q] = orc_two_stage(j->ptr, j->col, j->val, j->qptr, j->qcol, j->qval, j->rowscale,
+                                j->rows, j->cols, j->bits, j->quant, j->qq, j->split, j->ck, j->k,
+                                j->queries + (size_t)q * j->cols, j->out_idx + (size_t)q * j->k,
+                                j->out_score + (size_t)q * j->k, cand, &cn);
+  }
+  free(cand);
+  return NULL;
+}
+
+void orc_two_stage_many(const uint64_t* ptr, const uint32_t* col, const float* val,
+                        const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                        const float* rowscale, uint32_t rows, uint32_t cols, int bits, int quant,
+                        int qq, uint32_t split, uint32_t ck, uint32_t k, const float* queries,
+                        uint32_t nq, int nthreads, uint32_t* out_idx, float* out_score,
+                        uint32_t* out_n) {
+  if (nthreads < 1) nthreads = 1;
+  if ((uint32_t)nthreads > nq) nthreads = nq ? (int)nq : 1;
+  orc_tsjob_t* jobs = (orc_tsjob_t*)malloc(sizeof(orc_tsjob_t) * nthreads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+  for (int t = 0; t < nthreads; t++) {
+    orc_tsjob_t* j = &jobs[t];
+    j->ptr = ptr; j->col = col; j->val = val; j->qptr = qptr; j->qcol = qcol; j->qval = qval;
+    j->rowscale = rowscale; j->queries = queries; j->rows = rows; j->cols = cols;
+    j->split = split; j->ck = ck; j->k = k; j->bits = bits; j->quant = quant; j->qq = qq;
+    j->q0 = (uint32_t)((uint64_t)nq * t / nthreads);
+    j->q1 = (uint32_t)((uint64_t)nq * (t + 1) / nthreads);
+    j->out_idx = out_idx; j->out_score = out_score; j->out_n = out_n;
+    if (nthreads == 1) orc_ts_run(j);
+    else pthread_create(&th[t], NULL, orc_ts_run, j);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+}
+
+/* float64 Top-k of one query: a size-k min-heap on (score, -row), i.e. the k best by score
+ * descending with the lower row first among equal scores (numpy's stable argsort of -score). */
+typedef struct { double s; uint32_t r; } orc_sd_t;
+static int orc_sd_worse(orc_sd_t a, orc_sd_t b) { /* a ranks below b */
+  return a.s < b.s || (a.s == b.s && a.r > b.r);
+}
+static void orc_heap_down(orc_sd_t* h, uint32_t n, uint32_t i) {
+  for (;;) {
+    uint32_t l = 2 * i + 1, r = l + 1, m = i;
+    if (l < n && orc_sd_worse(h[l], h[m])) m = l;
+    if (r < n && orc_sd_worse(h[r], h[m])) m = r;
+    if (m == i) return;
+    orc_sd_t t = h[i]; h[i] = h[m]; h[m] = t;
+    i = m;
+  }
+}
+static int orc_sd_cmp_desc(const void* a, const void* b) {
+  orc_sd_t x = *(const orc_sd_t*)a, y = *(const orc_sd_t*)b;
+  if (orc_sd_worse(x, y)) return 1;
+  if (orc_sd_worse(y, x)) return -1;
+  return 0;
+}
+
+typedef struct {
+  const uint64_t* ptr;
+  const uint32_t* col;
+  const float *val, *queries;
+  uint32_t rows, cols, k, q0, q1;
+  uint32_t* out_idx;
+  double* out_score;
+} orc_f64job_t;
+
+static void* orc_f64_run(void* arg) {
+  orc_f64job_t* j = (orc_f64job_t*)arg;
+  orc_sd_t* h = (orc_sd_t*)malloc(sizeof(orc_sd_t) * (j->k ? j->k : 1));
+  for (uint32_t q = j->q0; q < j->q1; q++) {
+    const float* x = j->queries + (size_t)q * j->cols;
+    uint32_t n = 0;
+    for (uint32_t r = 0; r < j->rows; r++) {
+      double s = 0.0;
+      for (uint64_t e = j->ptr[r]; e < j->ptr[r + 1]; e++) s += (double)j->val[e] * (double)x[j->col[e]];
+      orc_sd_t c = {s, r};
+      if (n < j->k) {
+        h[n++] = c;
+        if (n == j->k)
+          for (int32_t i = (int32_t)n / 2 - 1; i >= 0; i--) orc_heap_down(h, n, (uint32_t)i);
+      } else if (orc_sd_worse(h[0], c)) {
+        h[0] = c;
+        orc_heap_down(h, n, 0);
+      }
+    }
+    qsort(h, n, sizeof(orc_sd_t), orc_sd_cmp_desc);
+    for (uint32_t i = 0; i < j->k; i++) {
+      j->out_idx[(size_t)q * j->k + i] = i < n ? h[i].r : 0xFFFFFFFFu;
+      j->out_score[(size_t)q * j->k + i] = i < n ? h[i].s : -INFINITY;
+    }
+  }
+  free(h);
+  return NULL;
+}
+
+void orc_topk_f64_many(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                       uint32_t cols, const float* queries, uint32_t nq, uint32_t k, int nthreads,
+                       uint32_t* out_idx, double* out_score) {
+  if (nthreads < 1) nthreads = 1;
+  if ((uint32_t)nthreads > nq) nthreads = nq ? (int)nq : 1;
+  orc_f64job_t* jobs = (orc_f64job_t*)malloc(sizeof(orc_f64job_t) * nthreads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+  for (int t = 0; t < nthreads; t++) {
+    orc_f64job_t* j = &jobs[t];
+    j->ptr = ptr; j->col = col; j->val = val; j->queries = queries;
+    j->rows = rows; j->cols = cols; j->k = k;
+    j->q0 = (uint32_t)((uint64_t)nq * t / nthreads);
+    j->q1 = (uint32_t)((uint64_t)nq * (t + 1) / nthreads);
+    j->out_idx = out_idx; j->out_score = out_score;
+    if (nthreads == 1) orc_f64_run(j);
+    else pthread_create(&th[t], NULL, orc_f64_run, j);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+}
+
+/* float64 score of the given (query, row) pairs: rows[q * k + i] of query q (0xFFFFFFFF: NaN). */
+void orc_rows_f64(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t cols,
+                  const float* queries, uint32_t nq, uint32_t k, const uint32_t* rows_sel,
+                  double* out) {
+  for (uint32_t q = 0; q < nq; q++) {
+    const float* x = queries + (size_t)q * cols;
+    for (uint32_t i = 0; i < k; i++) {
+      const uint32_t r = rows_sel[(size_t)q * k + i];
+      if (r == 0xFFFFFFFFu) { out[(size_t)q * k + i] = NAN; continue; }
+      double s = 0.0;
+      for (uint64_t e = ptr[r]; e < ptr[r + 1]; e++) s += (double)val[e] * (double)x[col[e]];
+      out[(size_t)q * k + i] = s;
+    }
+  }
+}

@@ -155,6 +155,34 @@ uint64_t orc_resparse(const uint64_t* ptr, const uint32_t* col, const float* val
                       uint32_t cols, double keep, uint64_t* out_ptr, uint32_t* out_col,
                       float* out_val);
 
+/* ---- seeded synthetic matrices and full-size checks ------------------------------------- */
+#define ORC_GEN_UNIFORM_DEG 0     /* degree U{p0..p1}, distinct uniform columns, values U(0,1) */
+#define ORC_GEN_FIXED_ABSNORMAL 1 /* degree p0, distinct uniform columns, values |N(0,1)| */
+#define ORC_GEN_GAMMA_DEG 2       /* degree min(p1, max(1, round(Gamma(2, p0/2)))), U(0,1) */
+#define ORC_GEN_FIXED_UNIFORM 3   /* degree p0, distinct uniform columns, values U(0,1) */
+/* The engine's seeded generator (aes_gen_matrix), restated so that the CPU baseline needs no
+ * engine library: a CSR sorted by (row, col), identical for the same arguments whatever the
+ * thread count.  ptr == NULL returns the nnz only; UINT64_MAX on bad arguments. */
+uint64_t orc_gen_matrix(uint32_t kind, uint32_t rows, uint32_t cols, double p0, double p1,
+                        uint64_t seed, int nthreads, uint64_t* ptr, uint32_t* col, float* val);
+/* orc_two_stage for nq queries [nq][cols] on nthreads threads: out_idx / out_score [nq][k],
+ * out_n[q] = results written for query q. */
+void orc_two_stage_many(const uint64_t* ptr, const uint32_t* col, const float* val,
+                        const uint64_t* qptr, const uint32_t* qcol, const int32_t* qval,
+                        const float* rowscale, uint32_t rows, uint32_t cols, int bits, int quant,
+                        int qq, uint32_t split, uint32_t ck, uint32_t k, const float* queries,
+                        uint32_t nq, int nthreads, uint32_t* out_idx, float* out_score,
+                        uint32_t* out_n);
+/* float64 Top-k of every row for nq queries (score descending, lower row first among equal
+ * scores: numpy's stable argsort of -score), nthreads threads; [nq][k] outputs. */
+void orc_topk_f64_many(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                       uint32_t cols, const float* queries, uint32_t nq, uint32_t k, int nthreads,
+                       uint32_t* out_idx, double* out_score);
+/* float64 scores of rows_sel[q][i] for query q ([nq][k]; row 0xFFFFFFFF gives NaN). */
+void orc_rows_f64(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t cols,
+                  const float* queries, uint32_t nq, uint32_t k, const uint32_t* rows_sel,
+                  double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,6 +126,23 @@ def lib():
         L.orc_bench_fp32_topk.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                           ctypes.c_uint32, _f32p, ctypes.c_uint32, ctypes.c_int,
                                           ctypes.c_double, _u32p]
+        L.orc_gen_matrix.restype = ctypes.c_uint64
+        L.orc_gen_matrix.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                     ctypes.c_int, _u64p, _u32p, _f32p]
+        L.orc_two_stage_many.restype = None
+        L.orc_two_stage_many.argtypes = [_u64p, _u32p, _f32p, _u64p, _u32p, _i32p, _f32p,
+                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
+                                         ctypes.c_uint32, ctypes.c_uint32, _f32p,
+                                         ctypes.c_uint32, ctypes.c_int, _u32p, _f32p, _u32p]
+        L.orc_topk_f64_many.restype = None
+        L.orc_topk_f64_many.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                        _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                        _u32p, _f64p]
+        L.orc_rows_f64.restype = None
+        L.orc_rows_f64.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, _f32p, ctypes.c_uint32,
+                                   ctypes.c_uint32, _u32p, _f64p]
         L.orc_resparse.restype = ctypes.c_uint64
         L.orc_resparse.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_double, _u64p, _u32p, _f32p]
@@ -354,6 +371,67 @@ class Matrix:
                                 self.bits, self.quant, qq, split, ck, k, _p(q, _f32p),
                                 _p(oi, _u32p), _p(os_, _f32p), _p(cand, _u32p), _p(cn, _u32p))
         return oi[:n].copy(), os_[:n].copy(), cand[: int(cn[0])].copy()
+
+
+GEN_UNIFORM_DEG = 0
+GEN_FIXED_ABSNORMAL = 1
+GEN_GAMMA_DEG = 2
+GEN_FIXED_UNIFORM = 3
+
+
+def gen_matrix(kind, rows, cols, p0, p1=0.0, seed=0, nthreads=None):
+    """The engine's seeded synthetic CSR (ptr u64, col u32, val f32), built by the oracle."""
+    L = lib()
+    nt = nthreads or (os.cpu_count() or 1)
+    nnz = L.orc_gen_matrix(kind, rows, cols, p0, p1, seed, nt, None, None, None)
+    if nnz == (1 << 64) - 1:
+        raise ValueError("bad generator arguments")
+    ptr = np.zeros(rows + 1, np.uint64)
+    col = np.zeros(max(nnz, 1), np.uint32)
+    val = np.zeros(max(nnz, 1), np.float32)
+    L.orc_gen_matrix(kind, rows, cols, p0, p1, seed, nt, _p(ptr, _u64p), _p(col, _u32p),
+                     _p(val, _f32p))
+    return ptr, col[:nnz], val[:nnz]
+
+
+def two_stage_many(m: "Matrix", queries, split, ck, k, qq=QQ_NUMPY, nthreads=None):
+    """Matrix.two_stage for every row of `queries` on host threads: (idx [nq, k], score [nq, k],
+    n [nq]); entries past n[q] are unset (row 0xFFFFFFFF, score -inf)."""
+    Q = np.ascontiguousarray(np.atleast_2d(queries), np.float32)
+    nq = Q.shape[0]
+    oi = np.full((nq, k), 0xFFFFFFFF, np.uint32)
+    os_ = np.full((nq, k), -np.inf, np.float32)
+    on = np.zeros(nq, np.uint32)
+    rs = m.rowscale if m.rowscale is not None else np.zeros(1, np.float32)
+    lib().orc_two_stage_many(_p(m.ptr, _u64p), _p(m.col, _u32p), _p(m.val, _f32p),
+                             _p(m.qptr, _u64p), _p(m.qcol, _u32p), _p(m.qval, _i32p),
+                             _p(rs, _f32p), m.rows, m.cols, m.bits, m.quant, qq, split, ck, k,
+                             _p(Q, _f32p), nq, nthreads or (os.cpu_count() or 1),
+                             _p(oi, _u32p), _p(os_, _f32p), _p(on, _u32p))
+    return oi, os_, on
+
+
+def topk_f64_many(ptr, col, val, rows, cols, queries, k, nthreads=None):
+    """float64 Top-k of every row per query: (idx [nq, k], score [nq, k]), score descending,
+    lower row first among equal scores."""
+    Q = np.ascontiguousarray(np.atleast_2d(queries), np.float32)
+    nq = Q.shape[0]
+    oi = np.zeros((nq, k), np.uint32)
+    os_ = np.zeros((nq, k), np.float64)
+    lib().orc_topk_f64_many(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                            _p(Q, _f32p), nq, k, nthreads or (os.cpu_count() or 1),
+                            _p(oi, _u32p), _p(os_, _f64p))
+    return oi, os_
+
+
+def rows_f64(ptr, col, val, cols, queries, rows_sel):
+    """float64 scores of rows_sel [nq, k] against queries [nq, cols] (NaN for row 0xFFFFFFFF)."""
+    Q = np.ascontiguousarray(np.atleast_2d(queries), np.float32)
+    R = np.ascontiguousarray(rows_sel, np.uint32)
+    out = np.zeros(R.shape, np.float64)
+    lib().orc_rows_f64(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), cols, _p(Q, _f32p),
+                       R.shape[0], R.shape[1], _p(R, _u32p), _p(out, _f64p))
+    return out
 
 
 def bench_two_stage(m: "Matrix", queries, ck, k, nthreads=1, max_seconds=10.0):

@@ -290,7 +290,8 @@ def make_mtx():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference/src")
+    ap.add_argument("--ref-src", default=os.environ.get("REF_SRC"), required="REF_SRC" not in os.environ,
+                    help="the reference's src directory (or set REF_SRC)")
     ap.add_argument("--only", default="quantify,split,gold,xdecode,resparse,mtx")
     args = ap.parse_args()
     only = set(args.only.split(","))

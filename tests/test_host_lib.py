@@ -219,3 +219,17 @@ def test_tensor_tile_layout_only_for_4bit_without_repeats():
     ptr2[6:] += 1
     tp, ent = E.pack_tc_host(ptr2, col2, val2, 300, 64, bits=4, quant=1, flags=E.FLAG_TENSOR)
     assert len(ent) == 0
+
+
+@pytest.mark.parametrize("kind,rows,cols,p0,p1", [
+    (E.GEN_UNIFORM_DEG, 5000, 1024, 10, 30), (E.GEN_FIXED_ABSNORMAL, 3000, 500, 69, 0),
+    (E.GEN_GAMMA_DEG, 4000, 1024, 32, 512), (E.GEN_FIXED_UNIFORM, 2000, 900, 108, 0),
+    (E.GEN_UNIFORM_DEG, 500, 64, 40, 60)])
+def test_oracle_generator_equals_engine_generator(kind, rows, cols, p0, p1):
+    # the CPU baseline builds its inputs with the oracle's copy of the generator; both must give
+    # the same matrix for the same arguments, whatever the thread count
+    a = E.gen_matrix(kind, rows, cols, p0, p1, seed=11)
+    for nt in (1, 3):
+        b = orc.gen_matrix(kind, rows, cols, p0, p1, seed=11, nthreads=nt)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
