@@ -1017,6 +1017,90 @@ void orc_topk_f64_many(const uint64_t* ptr, const uint32_t* col, const float* va
   free(th);
 }
 
+/* FP32 exact Top-k of every row (spmv_coo_gold_top_k's arithmetic, gold_algorithms.hpp:211-239:
+ * acc = acc + val * q[col] in column order, separately rounded), ordered as sort_tuples orders
+ * (score descending, row descending; evaluation_utils.hpp:40-62). */
+typedef struct { float s; uint32_t r; } orc_sf_t;
+static int orc_sf_worse(orc_sf_t a, orc_sf_t b) { return a.s < b.s || (a.s == b.s && a.r < b.r); }
+static void orc_heapf_down(orc_sf_t* h, uint32_t n, uint32_t i) {
+  for (;;) {
+    uint32_t l = 2 * i + 1, r = l + 1, m = i;
+    if (l < n && orc_sf_worse(h[l], h[m])) m = l;
+    if (r < n && orc_sf_worse(h[r], h[m])) m = r;
+    if (m == i) return;
+    orc_sf_t t = h[i]; h[i] = h[m]; h[m] = t;
+    i = m;
+  }
+}
+static int orc_sf_cmp_desc(const void* a, const void* b) {
+  orc_sf_t x = *(const orc_sf_t*)a, y = *(const orc_sf_t*)b;
+  if (orc_sf_worse(x, y)) return 1;
+  if (orc_sf_worse(y, x)) return -1;
+  return 0;
+}
+
+typedef struct {
+  const uint64_t* ptr;
+  const uint32_t* col;
+  const float *val, *queries;
+  uint32_t rows, cols, k, q0, q1;
+  uint32_t* out_idx;
+  float* out_score;
+} orc_f32job_t;
+
+static void* orc_f32_run(void* arg) {
+  orc_f32job_t* j = (orc_f32job_t*)arg;
+  orc_sf_t* h = (orc_sf_t*)malloc(sizeof(orc_sf_t) * (j->k ? j->k : 1));
+  for (uint32_t q = j->q0; q < j->q1; q++) {
+    const float* x = j->queries + (size_t)q * j->cols;
+    uint32_t n = 0;
+    for (uint32_t r = 0; r < j->rows; r++) {
+      float s = 0.0f;
+      for (uint64_t e = j->ptr[r]; e < j->ptr[r + 1]; e++) s = s + j->val[e] * x[j->col[e]];
+      if (s == 0.0f) s = 0.0f;
+      orc_sf_t c = {s, r};
+      if (n < j->k) {
+        h[n++] = c;
+        if (n == j->k)
+          for (int32_t i = (int32_t)n / 2 - 1; i >= 0; i--) orc_heapf_down(h, n, (uint32_t)i);
+      } else if (orc_sf_worse(h[0], c)) {
+        h[0] = c;
+        orc_heapf_down(h, n, 0);
+      }
+    }
+    qsort(h, n, sizeof(orc_sf_t), orc_sf_cmp_desc);
+    for (uint32_t i = 0; i < j->k; i++) {
+      j->out_idx[(size_t)q * j->k + i] = i < n ? h[i].r : 0xFFFFFFFFu;
+      j->out_score[(size_t)q * j->k + i] = i < n ? h[i].s : -INFINITY;
+    }
+  }
+  free(h);
+  return NULL;
+}
+
+void orc_topk_f32_many(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                       uint32_t cols, const float* queries, uint32_t nq, uint32_t k, int nthreads,
+                       uint32_t* out_idx, float* out_score) {
+  if (nthreads < 1) nthreads = 1;
+  if ((uint32_t)nthreads > nq) nthreads = nq ? (int)nq : 1;
+  orc_f32job_t* jobs = (orc_f32job_t*)malloc(sizeof(orc_f32job_t) * nthreads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+  for (int t = 0; t < nthreads; t++) {
+    orc_f32job_t* j = &jobs[t];
+    j->ptr = ptr; j->col = col; j->val = val; j->queries = queries;
+    j->rows = rows; j->cols = cols; j->k = k;
+    j->q0 = (uint32_t)((uint64_t)nq * t / nthreads);
+    j->q1 = (uint32_t)((uint64_t)nq * (t + 1) / nthreads);
+    j->out_idx = out_idx; j->out_score = out_score;
+    if (nthreads == 1) orc_f32_run(j);
+    else pthread_create(&th[t], NULL, orc_f32_run, j);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+}
+
 /* float64 score of the given (query, row) pairs: rows[q * k + i] of query q (0xFFFFFFFF: NaN). */
 void orc_rows_f64(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t cols,
                   const float* queries, uint32_t nq, uint32_t k, const uint32_t* rows_sel,

@@ -178,6 +178,10 @@ void orc_two_stage_many(const uint64_t* ptr, const uint32_t* col, const float* v
 void orc_topk_f64_many(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
                        uint32_t cols, const float* queries, uint32_t nq, uint32_t k, int nthreads,
                        uint32_t* out_idx, double* out_score);
+/* FP32 exact Top-k of every row (column-order FP32 sums, sort_tuples order), nthreads threads. */
+void orc_topk_f32_many(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
+                       uint32_t cols, const float* queries, uint32_t nq, uint32_t k, int nthreads,
+                       uint32_t* out_idx, float* out_score);
 /* float64 scores of rows_sel[q][i] for query q ([nq][k]; row 0xFFFFFFFF gives NaN). */
 void orc_rows_f64(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t cols,
                   const float* queries, uint32_t nq, uint32_t k, const uint32_t* rows_sel,

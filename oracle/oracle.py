@@ -140,6 +140,10 @@ def lib():
         L.orc_topk_f64_many.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                         _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                         _u32p, _f64p]
+        L.orc_topk_f32_many.restype = None
+        L.orc_topk_f32_many.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                        _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                        _u32p, _f32p]
         L.orc_rows_f64.restype = None
         L.orc_rows_f64.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, _f32p, ctypes.c_uint32,
                                    ctypes.c_uint32, _u32p, _f64p]
@@ -421,6 +425,19 @@ def topk_f64_many(ptr, col, val, rows, cols, queries, k, nthreads=None):
     lib().orc_topk_f64_many(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
                             _p(Q, _f32p), nq, k, nthreads or (os.cpu_count() or 1),
                             _p(oi, _u32p), _p(os_, _f64p))
+    return oi, os_
+
+
+def topk_f32_many(ptr, col, val, rows, cols, queries, k, nthreads=None):
+    """FP32 exact Top-k of every row per query (the reference's FP32 method, sort_tuples order):
+    (idx [nq, k], score [nq, k])."""
+    Q = np.ascontiguousarray(np.atleast_2d(queries), np.float32)
+    nq = Q.shape[0]
+    oi = np.zeros((nq, k), np.uint32)
+    os_ = np.zeros((nq, k), np.float32)
+    lib().orc_topk_f32_many(_p(ptr, _u64p), _p(col, _u32p), _p(val, _f32p), rows, cols,
+                            _p(Q, _f32p), nq, k, nthreads or (os.cpu_count() or 1),
+                            _p(oi, _u32p), _p(os_, _f32p))
     return oi, os_
 
 
