@@ -1,6 +1,8 @@
-// aes_batch.cuh -- batched candidate pass: one read of the Ultra-CSR matrix scores a tile of up
+// aes_batch.cuh -- batched candidate pass: one read of the Ultra-CSR matrix scores a block of up
 // to 128 queries (the reference's spmv_ucsr_top_k_main scores one query per pass,
-// spmv_ucsr_top_k_multicore.cpp:8-143).
+// spmv_ucsr_top_k_multicore.cpp:8-143).  One launch scores every block of a batch: blockIdx.y
+// is the block, so the blocks run as successive waves of CTAs, each CTA loading its block's
+// query table once.
 //
 // Per warp and 32-packet tile:
 //   phase A (lane = packet): decode the packet's flags, 10-bit columns and B-bit values into
@@ -31,17 +33,20 @@ struct BatchArgs {
   const uint4* tiles;
   const uint32_t* tile_rowbase;
   uint32_t n_tiles, n_rows, cols;
-  const uint32_t* qtab;         // [cols][33] words: bytes of queries 4l..4l+3 at (col, lane l)
-  uint32_t q0, nq;              // this launch scores queries q0 .. q0 + nq - 1 (nq <= 128)
+  const uint32_t* qtab;         // [blocks][cols][33] words: bytes of queries 128 b + 4l .. 4l+3 at
+                                // (col, lane l)
+  uint32_t nq;                  // queries of the batch (blocks = ceil(nq / 128))
+  uint32_t blk0;                // blocks blk0 .. blk0 + gridDim.y - 1 in this launch
   const float* rowscale;
   uint32_t split, slice;
-  const uint32_t* thr;          // [nq_total][split] (MODE_FILTER)
-  uint32_t* cnt;                // [nq_total][split]
-  uint2* surv;                  // [nq_total][split][cap]
+  const uint32_t* thr;          // [nq][split] (MODE_FILTER)
+  uint32_t* cnt;                // [nq][split]
+  uint2* surv;                  // [nq][split][cap]
   uint32_t cap;
-  uint32_t* keys_out;           // MODE_SAMPLE: [sample rows][128]
+  uint32_t* keys_out;           // MODE_SAMPLE: block b at keys_out + b * 128 * n_sample_rows,
+                                // [sample rows][128]
   const uint32_t* sample_first;
-  uint32_t sample_stride, n_sample_tiles;
+  uint32_t sample_stride, n_sample_tiles, n_sample_rows;
 };
 
 // per-warp element records: columns (u32), values (u8) and row flags (u8) of the 32
@@ -99,6 +104,8 @@ struct BatchRows {
   int32_t thr_sc[4];      // split == 1, integer keys: thr4 as signed score bounds
   uint32_t sample_base;
   uint32_t lane;
+  uint32_t q0, nq;        // the block's queries q0 .. q0 + nq - 1
+  uint32_t* keys_blk;     // MODE_SAMPLE: the block's key array
 
   // the four queries of this lane finished row `row` with integer scores acc[0..3]
   __device__ __forceinline__ void finish(uint32_t row, const int32_t (&acc)[4]) const {
@@ -121,7 +128,7 @@ struct BatchRows {
       for (int t = 0; t < 4; t++) key[t] = key_i32(acc[t]);
     }
     if constexpr (MODE == MODE_SAMPLE) {
-      reinterpret_cast<uint4*>(a.keys_out)[(size_t)(row - sample_base) * 32 + lane] =
+      reinterpret_cast<uint4*>(keys_blk)[(size_t)(row - sample_base) * 32 + lane] =
           make_uint4(key[0], key[1], key[2], key[3]);
     } else if constexpr (MODE == MODE_FILTER) {
       const uint32_t p = part_of(row, a.split, a.slice);
@@ -136,7 +143,7 @@ struct BatchRows {
 #pragma unroll
         for (int t = 0; t < 4; t++) {
           const uint32_t q = 4 * lane + t;
-          th[t] = q < a.nq ? __ldg(a.thr + (size_t)(a.q0 + q) * a.split + p) : 0xFFFFFFFFu;
+          th[t] = q < nq ? __ldg(a.thr + (size_t)(q0 + q) * a.split + p) : 0xFFFFFFFFu;
         }
       }
       const bool hit = (key[0] >= th[0]) | (key[1] >= th[1]) | (key[2] >= th[2]) | (key[3] >= th[3]);
@@ -154,7 +161,7 @@ struct BatchRows {
     if (a.split <= 1) return thr4[t];
     if (thr_s) return thr_s[p * kBatchQ + 4 * lane + t];
     const uint32_t q = 4 * lane + t;
-    return q < a.nq ? __ldg(a.thr + (size_t)(a.q0 + q) * a.split + p) : 0xFFFFFFFFu;
+    return q < nq ? __ldg(a.thr + (size_t)(q0 + q) * a.split + p) : 0xFFFFFFFFu;
   }
   // integer keys: per query, the lowest score bound over the partitions of rows r0 .. r1 (one
   // partition for almost every tile: the partitions are contiguous row ranges)
@@ -192,8 +199,8 @@ struct BatchRows {
     for (int t = 0; t < 4; t++) {
       const uint32_t key = is_key ? (uint32_t)v[t] : key_i32(v[t]);
       const uint32_t q = 4 * lane + t;
-      if (key >= th[t] && q < a.nq) {
-        const size_t qp = (size_t)(a.q0 + q) * a.split + p;
+      if (key >= th[t] && q < nq) {
+        const size_t qp = (size_t)(q0 + q) * a.split + p;
         const uint32_t i = atomicAdd(a.cnt + qp, 1u);
         if (i < a.cap) a.surv[qp * a.cap + i] = make_uint2(key, row);
       }
@@ -371,8 +378,16 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
     wsm[(size_t)NR * 4 + NR - 4 + lane] = 0u;
     wsm[(size_t)NR * 5 + NR - 4 + lane] = 0u;
   }
+  const uint32_t wpc = blockDim.x >> 5;
+  const uint32_t gw = blockIdx.x * wpc + warp;
+  const uint32_t nwp = gridDim.x * wpc;
+  // blockIdx.y selects the block of 128 queries: the blocks of a batch run as successive waves
+  // of one launch, each CTA loading its block's query table once
+  const uint32_t blk = a.blk0 + blockIdx.y;
+  const uint32_t q0 = blk * kBatchQ;
+  const uint32_t nq = min((uint32_t)kBatchQ, a.nq - q0);
   {
-    const uint4* src = reinterpret_cast<const uint4*>(a.qtab);
+    const uint4* src = reinterpret_cast<const uint4*>(a.qtab + (size_t)blk * batch_qtab_words(a.cols));
     uint4* dst = reinterpret_cast<uint4*>(qtb);
     // eight independent loads per thread in flight: the fill is latency-bound otherwise
     const uint32_t n = (uint32_t)(qtab_bytes / 16);
@@ -381,7 +396,7 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
 #pragma unroll
       for (int u = 0; u < 8; u++) {
         const uint32_t i = i0 + u * blockDim.x + threadIdx.x;
-        if (i < n) v[u] = src[i];
+        if (i < n) v[u] = __ldg(src + i);
       }
 #pragma unroll
       for (int u = 0; u < 8; u++) {
@@ -391,27 +406,26 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
     }
   }
   BatchRows<MODE> rows{a, nullptr, {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu},
-                       {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF}, 0u, lane};
+                       {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF}, 0u, lane, q0, nq,
+                       MODE == MODE_SAMPLE ? a.keys_out + (size_t)blk * kBatchQ * a.n_sample_rows
+                                           : nullptr};
   if constexpr (MODE == MODE_FILTER) {
     if (thr_in_smem) {
       for (uint32_t i = threadIdx.x; i < a.split * kBatchQ; i += blockDim.x) {
         const uint32_t p = i / kBatchQ, q = i % kBatchQ;
-        thr_s[i] = q < a.nq ? a.thr[(size_t)(a.q0 + q) * a.split + p] : 0xFFFFFFFFu;
+        thr_s[i] = q < nq ? a.thr[(size_t)(q0 + q) * a.split + p] : 0xFFFFFFFFu;
       }
       rows.thr_s = thr_s;
     } else if (a.split <= 1) {
 #pragma unroll
       for (int t = 0; t < 4; t++) {
         const uint32_t q = 4 * lane + t;
-        rows.thr4[t] = q < a.nq ? a.thr[(size_t)(a.q0 + q) * a.split] : 0xFFFFFFFFu;
+        rows.thr4[t] = q < nq ? a.thr[(size_t)(q0 + q) * a.split] : 0xFFFFFFFFu;
         rows.thr_sc[t] = (int32_t)(rows.thr4[t] ^ 0x80000000u);
       }
     }
   }
   __syncthreads();
-  const uint32_t wpc = blockDim.x >> 5;
-  const uint32_t gw = blockIdx.x * wpc + warp;
-  const uint32_t nwp = gridDim.x * wpc;
   if constexpr (MODE == MODE_SAMPLE) {
     for (uint32_t s = gw; s < a.n_sample_tiles; s += nwp) {
       const uint32_t t = s * a.sample_stride;
@@ -426,15 +440,19 @@ __global__ void __launch_bounds__(kWarpsBatchMax * 32, 1) k_cand_batch(BatchArgs
   }
 }
 
-// Sample keys of one batched block, [rows][128 queries] as the batched sample pass writes them,
-// to [query][rows] (the plain layout), so the threshold pass reads each query's keys
-// contiguously instead of one 32-byte sector per key.  A CTA moves 32 rows x 128 queries through
-// shared memory; both the reads and the writes are coalesced.
+// Sample keys of the batched blocks, [rows][128 queries] per block as the batched sample pass
+// writes them, to [query][rows] (the plain layout), so the threshold pass reads each query's keys
+// contiguously instead of one 32-byte sector per key.  A CTA moves 32 rows x 128 queries of one
+// block (blockIdx.y) through shared memory; both the reads and the writes are coalesced.
 constexpr uint32_t kTransposeRows = 32;
 __global__ void __launch_bounds__(256) k_keys_transpose(const uint32_t* __restrict__ in,
                                                         uint32_t n_rows, uint32_t nq,
                                                         uint32_t* __restrict__ out) {
   __shared__ uint32_t t[kTransposeRows][kBatchQ + 1];
+  const uint32_t blk = blockIdx.y;
+  const uint32_t nb = min((uint32_t)kBatchQ, nq - blk * kBatchQ);
+  in += (size_t)blk * kBatchQ * n_rows;
+  out += (size_t)blk * kBatchQ * n_rows;
   const uint32_t r0 = blockIdx.x * kTransposeRows;
   for (uint32_t i = threadIdx.x; i < kTransposeRows * kBatchQ; i += blockDim.x) {
     const uint32_t rr = i / kBatchQ, q = i % kBatchQ;
@@ -443,23 +461,28 @@ __global__ void __launch_bounds__(256) k_keys_transpose(const uint32_t* __restri
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < kTransposeRows * kBatchQ; i += blockDim.x) {
     const uint32_t q = i / kTransposeRows, rr = i % kTransposeRows;
-    if (q < nq && r0 + rr < n_rows) out[(size_t)q * n_rows + r0 + rr] = t[rr][q];
+    if (q < nb && r0 + rr < n_rows) out[(size_t)q * n_rows + r0 + rr] = t[rr][q];
   }
 }
 
-// qtab[col][33] words: byte t of word (col, l) = quantised query q0 + 4l + t at col (0 past nq);
-// word 32 of each column and the padding to a 16-byte slot are zero
-__global__ void k_qtable(const int8_t* __restrict__ q8, uint32_t ld8, uint32_t cols, uint32_t q0,
-                         uint32_t nq, uint32_t* __restrict__ qtab) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= batch_qtab_words(cols)) return;
-  const uint32_t c = i / kQtabWords, l = i % kQtabWords;
+// qtab[blk][col][33] words: byte t of word (blk, col, l) = quantised query 128 blk + 4l + t at
+// col (0 past nq); word 32 of each column and the padding to a 16-byte slot are zero.  Every
+// block of the batch in one launch.
+__global__ void k_qtable(const int8_t* __restrict__ q8, uint32_t ld8, uint32_t cols, uint32_t nq,
+                         uint32_t* __restrict__ qtab) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nblk = (nq + kBatchQ - 1) / kBatchQ;
+  const uint64_t per = batch_qtab_words(cols);
+  if (i >= nblk * per) return;
+  const uint32_t blk = (uint32_t)(i / per);
+  const uint32_t r = (uint32_t)(i % per);
+  const uint32_t c = r / kQtabWords, l = r % kQtabWords;
   uint32_t w = 0;
   if (c < cols && l < 32u) {
 #pragma unroll
     for (int t = 0; t < 4; t++) {
-      const uint32_t q = 4 * l + t;
-      const uint32_t b = q < nq ? (uint32_t)(uint8_t)q8[(size_t)(q0 + q) * ld8 + c] : 0u;
+      const uint32_t q = blk * kBatchQ + 4 * l + t;
+      const uint32_t b = q < nq ? (uint32_t)(uint8_t)q8[(size_t)q * ld8 + c] : 0u;
       w |= b << (8 * t);
     }
   }

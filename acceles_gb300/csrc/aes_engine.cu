@@ -268,7 +268,7 @@ struct Engine {
   int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y = 1);
-  int run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s);
+  int run_batch(int mode, uint32_t nq, cudaStream_t s, uint32_t blk0 = 0, uint32_t nblk = 0);
   int run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s);
   int prof_open(cudaStream_t s);
   int prof_close(cudaStream_t s);
@@ -727,16 +727,19 @@ int Engine::run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y) {
   return AES_OK;
 }
 
-int Engine::run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
+// The batched pass of mode over every 128-query block of an nq-query batch in one persistent
+// launch (blocks walked one after another; each CTA loads a block's query table once)
+int Engine::run_batch(int mode, uint32_t nq, cudaStream_t s, uint32_t blk0, uint32_t nblk) {
   BatchArgs a{};
   a.tiles = d_tiles;
   a.tile_rowbase = d_tile_rowbase;
   a.n_tiles = (uint32_t)tiles;
   a.n_rows = rows;
   a.cols = cols;
-  a.qtab = d_qtab + (size_t)blk * batch_qtab_words(cols);
-  a.q0 = blk * kBatchQ;
-  a.nq = nq_blk;
+  a.qtab = d_qtab;
+  a.nq = nq;
+  a.blk0 = blk0;
+  if (!nblk) nblk = (nq + kBatchQ - 1) / kBatchQ - blk0;
   a.rowscale = d_rowscale;
   a.split = split;
   a.slice = slice;
@@ -744,10 +747,11 @@ int Engine::run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
   a.cnt = d_cnt;
   a.surv = d_surv;
   a.cap = cap;
-  a.keys_out = d_sample_keys + (size_t)blk * kBatchQ * n_sample_rows;
+  a.keys_out = d_sample_keys;
   a.sample_first = d_sample_first;
   a.sample_stride = ss;
   a.n_sample_tiles = n_sample_tiles;
+  a.n_sample_rows = n_sample_rows;
   int grid = batch_grid;
   if (mode == MODE_SAMPLE)
     grid = std::min<int>(grid, (int)((n_sample_tiles + batch_warps_n - 1) / batch_warps_n));
@@ -755,7 +759,7 @@ int Engine::run_batch(int mode, uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
   const bool prof = (prm.flags & AES_FLAG_PROFILE) && mode != MODE_SAMPLE;
   int rc = prof ? prof_open(s) : AES_OK;
   if (rc) return rc;
-  pick_batch((int)bits, sgn, mode)<<<grid, batch_warps_n * 32, batch_smem, s>>>(a);
+  pick_batch((int)bits, sgn, mode)<<<dim3(grid, nblk), batch_warps_n * 32, batch_smem, s>>>(a);
   AES_CK(cudaGetLastError());
   if (prof && (rc = prof_close(s))) return rc;
   n_launch++;
@@ -774,21 +778,21 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   last_batched = batched;
   const uint32_t nblk = (nq + kBatchQ - 1) / kBatchQ;
   if (batched) {
-    for (uint32_t b = 0; b < nblk; b++) {
-      const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
-      k_qtable<<<(uint32_t)((batch_qtab_words(cols) + 255) / 256), 256, 0, s>>>(
-          d_q8, ld8, cols, b * kBatchQ, nb, d_qtab + (size_t)b * batch_qtab_words(cols));
-      AES_CK(cudaGetLastError());
-      n_launch++;
-      if (use_tc) {
+    k_qtable<<<(uint32_t)((nblk * batch_qtab_words(cols) + 255) / 256), 256, 0, s>>>(
+        d_q8, ld8, cols, nq, d_qtab);
+    AES_CK(cudaGetLastError());
+    n_launch++;
+    if (use_tc) {
+      for (uint32_t b = 0; b < nblk; b++) {
+        const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
         k_qtable_tc<<<(kTcQ * tc_kpad(cols) + 255) / 256, 256, 0, s>>>(
             d_q8, ld8, cols, b * kTcQ, nb, d_qtab_tc + (size_t)b * tc_qtab_bytes(cols));
         AES_CK(cudaGetLastError());
         n_launch++;
       }
-      int rc = run_batch(MODE_SAMPLE, b, nb, s);
-      if (rc) return rc;
     }
+    int rc = run_batch(MODE_SAMPLE, nq, s);
+    if (rc) return rc;
   } else {
     for (uint32_t q0 = 0; q0 < nq; q0 += 65535u) {  // every query's sample pass in one launch
       int rc = run_plain(MODE_SAMPLE, q0, s, std::min<uint32_t>(65535u, nq - q0));
@@ -796,22 +800,23 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
     }
   }
   if (batched && n_sample_rows) {  // the threshold pass reads each query's keys contiguously
-    for (uint32_t b = 0; b < nblk; b++) {
-      const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
-      const size_t off = (size_t)b * kBatchQ * n_sample_rows;
-      k_keys_transpose<<<(n_sample_rows + kTransposeRows - 1) / kTransposeRows, 256, 0, s>>>(
-          d_sample_keys + off, n_sample_rows, nb, d_keys_t + off);
-      AES_CK(cudaGetLastError());
-      n_launch++;
-    }
+    k_keys_transpose<<<dim3((n_sample_rows + kTransposeRows - 1) / kTransposeRows, nblk), 256, 0, s>>>(
+        d_sample_keys, n_sample_rows, nq, d_keys_t);
+    AES_CK(cudaGetLastError());
+    n_launch++;
   }
   k_threshold<<<dim3(split, nq), kThreadsThr, 0, s>>>(batched ? d_keys_t : d_sample_keys, n_sample_rows, 0,
                                               d_part_sample_begin, split, d_part_r, d_thr, d_cnt);
   AES_CK(cudaGetLastError());
   if (batched) {
-    for (uint32_t b = 0; b < nblk; b++) {
-      const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
-      int rc = use_tc ? run_tc(b, nb, s) : run_batch(MODE_FILTER, b, nb, s);
+    if (use_tc) {
+      for (uint32_t b = 0; b < nblk; b++) {
+        const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
+        int rc = run_tc(b, nb, s);
+        if (rc) return rc;
+      }
+    } else {
+      int rc = run_batch(MODE_FILTER, nq, s);
       if (rc) return rc;
     }
   } else {
