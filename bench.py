@@ -86,12 +86,12 @@ def profile_current(name):
     return bool(m) and m.group(1) == source_digest(PROFILE_SOURCES[name])
 
 
-def profile_traffic(name):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if it was
-    captured from the current kernel sources."""
+def profile_traffic(name, key="traffic_bytes_per_launch"):
+    """DRAM bytes per launch (or per `key`'s unit) of the dominant kernel from the committed ncu
+    summary, if it was captured from the current kernel sources."""
     if not profile_current(name):
         return None
-    v = profile_number(name, "traffic_bytes_per_launch")
+    v = profile_number(name, key)
     return int(v) if v is not None else None
 
 
@@ -553,7 +553,7 @@ def main():
     plain_alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS
     plain_achieved = plain_alg / (plain_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic("cand_batch_10Mx1024_b8.md")
+    traffic = profile_traffic("cand_batch_10Mx1024_b8.md", "traffic_bytes_per_block")
     # the batched pass is bound by instruction issue, not HBM: warp instructions per group of
     # four entries (ncu instruction count of the capture) x the groups of one block, over the
     # live time per block at the sampled SM clock; an SM issues at most 4 warp instructions a cycle

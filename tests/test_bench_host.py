@@ -11,7 +11,7 @@ import bench  # noqa: E402
 
 
 def test_profiles_carry_the_bench_figures():
-    t_batch = bench.profile_traffic("cand_batch_10Mx1024_b8.md")
+    t_batch = bench.profile_traffic("cand_batch_10Mx1024_b8.md", "traffic_bytes_per_block")
     t_plain = bench.profile_traffic("cand_pass_10Mx1024_b8.md")
     ipg = bench.profile_number("cand_batch_10Mx1024_b8.md", "warp_instructions_per_group")
     # a 10M x 1024 8-bit launch reads about 491 MB of packets
