@@ -21,6 +21,7 @@
 #include "acceles.h"
 #include "aes_host.hpp"
 #include "aes_kernels.cuh"
+#include "aes_select.cuh"
 #include "aes_batch.cuh"
 #include "aes_tc.cuh"
 
@@ -111,6 +112,7 @@ struct Engine {
   uint32_t* d_csr_ptr = nullptr;
   uint16_t* d_csr_col = nullptr;
   float* d_csr_val = nullptr;
+  bool has_f32 = true;  // FP32 values resident: the exact pass can run
 
   // ---- configuration: selection geometry and per-batch buffers (aes_retune may change these) --
   struct Config {
@@ -149,8 +151,12 @@ struct Engine {
   uint32_t* d_exact_key = nullptr;
 
   float* h_q32 = nullptr;         // pinned staging of queries
+  int8_t* h_q8 = nullptr;         // pinned staging of pre-quantised queries
   uint32_t* h_status = nullptr;   // pinned
   uint32_t nq_loaded = 0;
+  bool q_pre = false;             // the loaded queries were given quantised
+  bool q32_given = true;          // ... with their FP32 values (for the exact pass)
+  bool last_int_final = false;    // the last run ranked its candidates by integer score
   uint32_t last_nq = 0, last_k = 0;
   bool last_from_device = false;
   const float* last_q32 = nullptr;   // query buffer of the last run
@@ -166,8 +172,10 @@ struct Engine {
     uint32_t* idx;
     float* score;
     cudaStream_t s;
+    bool pre;
     bool operator<(const GraphKey& o) const {
-      return std::tie(q, nq, k, idx, score, s) < std::tie(o.q, o.nq, o.k, o.idx, o.score, o.s);
+      return std::tie(q, nq, k, idx, score, s, pre) <
+             std::tie(o.q, o.nq, o.k, o.idx, o.score, o.s, o.pre);
     }
   };
   std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -209,8 +217,10 @@ struct Engine {
     for (void* p : cfg_allocs) cudaFree(p);
     cfg_allocs.clear();
     if (h_q32) cudaFreeHost(h_q32);
+    if (h_q8) cudaFreeHost(h_q8);
     if (h_status) cudaFreeHost(h_status);
     h_q32 = nullptr;
+    h_q8 = nullptr;
     h_status = nullptr;
     d_sample_first = d_part_sample_begin = d_part_r = nullptr;
     d_q32 = nullptr;
@@ -261,10 +271,14 @@ struct Engine {
   int plan_config(const aes_params& p, Config* c) const;
   int apply_config(const Config& c);
   int retune(const aes_params& p);
+  // d_q: the FP32 queries, or null when there are none (pre-quantised queries alone); pre: the
+  // quantised queries are already in d_q8
   int enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
-              cudaStream_t s);
+              cudaStream_t s, bool pre = false);
   int enqueue_graph(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
-                    cudaStream_t s);
+                    cudaStream_t s, bool pre = false);
+  // the final Top-K ranks the candidates by integer score: no FP32 values or no FP32 queries
+  bool int_final(const float* d_q) const { return !has_f32 || d_q == nullptr; }
   int repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cudaStream_t s,
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y = 1);
@@ -351,10 +365,11 @@ int Engine::collect_profile() {
 
 // Device bytes of the matrix itself: Ultra-CSR tiles, tile row bases, per-row scales, the FP32
 // CSR of the exact pass and the slow path's key array.
-static size_t matrix_plan(uint64_t tiles, uint32_t rows, uint64_t nnz, uint32_t quant) {
+static size_t matrix_plan(uint64_t tiles, uint32_t rows, uint64_t nnz, uint32_t quant,
+                          bool has_f32) {
   size_t plan = tiles * (size_t)kTileBytes + (tiles + 1) * 4;
   plan += (quant == AES_QUANT_UNSIGNED_ROW) ? rows * 4ull : 0;
-  plan += (rows + 1) * 4ull + nnz * 6ull;
+  plan += has_f32 ? (rows + 1) * 4ull + nnz * 6ull : 0;
   plan += rows * 4ull;
   return plan;
 }
@@ -494,6 +509,7 @@ int Engine::apply_config(const Config& c) {
   AES_AL(d_exact_aux, 4);
 #undef AES_AL
   AES_CK(cudaMallocHost(&h_q32, (size_t)maxB * ld32 * sizeof(float)));
+  AES_CK(cudaMallocHost(&h_q8, (size_t)maxB * ld8));
   AES_CK(cudaMallocHost(&h_status, (size_t)maxB * sizeof(uint32_t)));
   if (n_sample_tiles)
     AES_CK(cudaMemcpy(d_sample_first, c.sample_first.data(), n_sample_tiles * 4ull, cudaMemcpyHostToDevice));
@@ -556,6 +572,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   quant = p.quant;
   sgn = (quant == AES_QUANT_SYM_GLOBAL);
   nnz = m.ptr[rows];
+  has_f32 = !m.prequantized || m.val.size() == nnz;
   if (nnz >= 0xFFFFFFFFull) return fail(AES_ERR_UNSUPPORTED, "nnz must be below 2^32");
   ld32 = (cols + 3) & ~3u;
   ld8 = (cols + 15) & ~15u;
@@ -579,7 +596,7 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   if (rc) return rc;
 
   // ---- memory plan and admission: nothing is allocated unless all of it fits ---------------
-  const size_t plan = matrix_plan(tiles, rows, nnz, quant) + tc_bytes + c.plan;
+  const size_t plan = matrix_plan(tiles, rows, nnz, quant, has_f32) + tc_bytes + c.plan;
   if (p.mem_limit && plan > p.mem_limit)
     return fail(AES_ERR_NOMEM, "matrix needs " + std::to_string(plan) +
                                    " device bytes, over the handle limit " +
@@ -595,9 +612,11 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   AES_AL(d_tiles, tiles * 128);
   AES_AL(d_tile_rowbase, tiles + 1);
   if (quant == AES_QUANT_UNSIGNED_ROW) AES_AL(d_rowscale, rows);
-  AES_AL(d_csr_ptr, rows + 1);
-  AES_AL(d_csr_col, std::max<uint64_t>(nnz, 1));
-  AES_AL(d_csr_val, std::max<uint64_t>(nnz, 1));
+  if (has_f32) {
+    AES_AL(d_csr_ptr, rows + 1);
+    AES_AL(d_csr_col, std::max<uint64_t>(nnz, 1));
+    AES_AL(d_csr_val, std::max<uint64_t>(nnz, 1));
+  }
   AES_AL(d_allkeys, rows);
   if (tc_ready) {
     AES_AL(d_tc_ptr, pm.tc_ptr.size());
@@ -606,17 +625,19 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
 #undef AES_AL
 
   // ---- upload -----------------------------------------------------------------------------------
-  std::vector<uint32_t> ptr32(rows + 1);
-  std::vector<uint16_t> col16(nnz);
-  for (uint32_t r = 0; r <= rows; r++) ptr32[r] = (uint32_t)m.ptr[r];
-  parallel_for(nnz, 1 << 20, [&](uint64_t b, uint64_t e) {
-    for (uint64_t i = b; i < e; i++) col16[i] = (uint16_t)m.col[i];
-  });
+  std::vector<uint32_t> ptr32(has_f32 ? rows + 1 : 0);
+  std::vector<uint16_t> col16(has_f32 ? nnz : 0);
+  if (has_f32) {
+    for (uint32_t r = 0; r <= rows; r++) ptr32[r] = (uint32_t)m.ptr[r];
+    parallel_for(nnz, 1 << 20, [&](uint64_t b, uint64_t e) {
+      for (uint64_t i = b; i < e; i++) col16[i] = (uint16_t)m.col[i];
+    });
+  }
   AES_CK(cudaMemcpy(d_tiles, pm.tile_bytes.data(), pm.tile_bytes.size(), cudaMemcpyHostToDevice));
   AES_CK(cudaMemcpy(d_tile_rowbase, pm.tile_rowbase.data(), (tiles + 1) * 4, cudaMemcpyHostToDevice));
   if (d_rowscale) AES_CK(cudaMemcpy(d_rowscale, pm.rowscale.data(), rows * 4ull, cudaMemcpyHostToDevice));
-  AES_CK(cudaMemcpy(d_csr_ptr, ptr32.data(), (rows + 1) * 4ull, cudaMemcpyHostToDevice));
-  if (nnz) {
+  if (has_f32) AES_CK(cudaMemcpy(d_csr_ptr, ptr32.data(), (rows + 1) * 4ull, cudaMemcpyHostToDevice));
+  if (has_f32 && nnz) {
     AES_CK(cudaMemcpy(d_csr_col, col16.data(), nnz * 2, cudaMemcpyHostToDevice));
     AES_CK(cudaMemcpy(d_csr_val, m.val.data(), nnz * 4, cudaMemcpyHostToDevice));
   }
@@ -768,12 +789,15 @@ int Engine::run_batch(int mode, uint32_t nq, cudaStream_t s, uint32_t blk0, uint
 }
 
 int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool pre) {
   AES_CK(cudaMemsetAsync(d_status, 0, nq * 4ull, s));
-  k_quantize<<<nq, 256, 0, s>>>(d_q, cols, ld32, (int)bits, (int)quant,
-                                (int)prm.query_quant, d_q8, ld8, d_status);
-  AES_CK(cudaGetLastError());
-  n_launch += 4;  // quantise, threshold, select, final
+  if (!pre) {
+    k_quantize<<<nq, 256, 0, s>>>(d_q, cols, ld32, (int)bits, (int)quant,
+                                  (int)prm.query_quant, d_q8, ld8, d_status);
+    AES_CK(cudaGetLastError());
+    n_launch++;
+  }
+  n_launch += 3;  // threshold, select, final
   const bool batched = batch_mode != 1 && (batch_mode != 0 || nq >= 16);
   last_batched = batched;
   const uint32_t nblk = (nq + kBatchQ - 1) / kBatchQ;
@@ -852,6 +876,7 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   fa.out_idx = d_idx;
   fa.out_score = d_score;
   fa.status = d_status;
+  fa.cand_key = int_final(d_q) ? d_cand_key : nullptr;
   k_final<<<nq, kThreadsFinal, final_smem, s>>>(fa);
   AES_CK(cudaGetLastError());
   return AES_OK;
@@ -860,8 +885,8 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
 // Replays the launch sequence of enqueue() as one CUDA graph (captured on first use for these
 // arguments).  Profiling events are not recorded inside graphs.
 int Engine::enqueue_graph(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx,
-                          float* d_score, cudaStream_t s) {
-  GraphKey key{d_q, nq, k, d_idx, d_score, s};
+                          float* d_score, cudaStream_t s, bool pre) {
+  GraphKey key{d_q, nq, k, d_idx, d_score, s, pre};
   auto it = graphs.find(key);
   if (it == graphs.end()) {
     if (graphs.size() >= 64) {
@@ -872,7 +897,7 @@ int Engine::enqueue_graph(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d
     prm.flags &= ~AES_FLAG_PROFILE;
     const uint64_t saved_launch = n_launch, saved_cand = n_cand;
     AES_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue(d_q, nq, k, d_idx, d_score, s);
+    int rc = enqueue(d_q, nq, k, d_idx, d_score, s, pre);
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
     prm.flags = saved_flags;
@@ -934,7 +959,7 @@ int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cud
     fa.csr_ptr = d_csr_ptr;
     fa.csr_col = d_csr_col;
     fa.csr_val = d_csr_val;
-    fa.q32 = last_q32 + (size_t)q * ld32;
+    fa.q32 = last_q32 ? last_q32 + (size_t)q * ld32 : nullptr;
     fa.ld32 = ld32;
     fa.cols = cols;
     fa.cand = d_cand + (size_t)q * nslots;
@@ -944,6 +969,7 @@ int Engine::repair(uint32_t nq, uint32_t k, uint32_t* d_idx, float* d_score, cud
     fa.out_idx = d_idx + (size_t)q * k;
     fa.out_score = d_score + (size_t)q * k;
     fa.status = nullptr;
+    fa.cand_key = last_int_final ? d_cand_key + (size_t)q * nslots : nullptr;
     k_final<<<1, kThreadsFinal, final_smem, s>>>(fa);
     AES_CK(cudaGetLastError());
   }
@@ -1051,6 +1077,24 @@ int aes_create_csr(const uint64_t* ptr, const uint32_t* col, const float* val, u
   return create_common(m, p, out);
 }
 
+int aes_create_quantized(const uint32_t* row, const uint32_t* col, const int8_t* q_val,
+                         const float* val, uint32_t rows, uint32_t cols, uint64_t nnz,
+                         const aes_params* p, aes_handle** out) {
+  if (!out) return aes::fail(AES_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate_params(p, rows, cols);
+  if (rc) return rc;
+  if (p->quant != AES_QUANT_SYM_GLOBAL)
+    return aes::fail(AES_ERR_UNSUPPORTED, "pre-quantised matrices take the symmetric B-bit values");
+  if (nnz && (!row || !col || !q_val)) return aes::fail(AES_ERR_INVALID, "NULL COO array");
+  aes::HostCSR m;
+  rc = aes::coo_to_csr(row, col, val, rows, cols, nnz, &m, q_val);
+  if (rc) return rc;
+  m.prequantized = true;
+  if (!val) m.val.clear();
+  return create_common(m, p, out);
+}
+
 int aes_pack_host(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
                   uint32_t cols, const aes_params* p, uint8_t* packets, uint64_t cap_packets,
                   uint64_t* n_packets, uint32_t* tile_rowbase) {
@@ -1145,6 +1189,7 @@ int aes_get_info(const aes_handle* h, aes_info* info) {
   info->max_batch = e.maxB;
   info->batch_tile = e.batch_mode == 1 ? 1 : aes::dev::kBatchQ;
   info->tensor_tiles = e.use_tc ? 1u : 0u;
+  info->exact_pass = e.has_f32 ? 1u : 0u;
   return AES_OK;
 }
 
@@ -1157,6 +1202,37 @@ int aes_set_query(aes_handle* h, const float* q, uint32_t nq) {
   for (uint32_t i = 0; i < nq; i++) std::memcpy(e.h_q32 + (size_t)i * e.ld32, q + (size_t)i * e.cols, e.cols * 4ull);
   AES_CK(cudaMemcpyAsync(e.d_q32, e.h_q32, (size_t)nq * e.ld32 * 4, cudaMemcpyHostToDevice, e.stream));
   e.nq_loaded = nq;
+  e.q_pre = false;
+  e.q32_given = true;
+  return AES_OK;
+}
+
+int aes_set_query_quantized(aes_handle* h, const int8_t* q, const float* q_f32, uint32_t nq) {
+  if (!h || !q) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  Engine& e = h->e;
+  if (!e.configured) return aes::fail(AES_ERR_STATE, kUnconfigured);
+  if (nq == 0 || nq > e.maxB) return aes::fail(AES_ERR_INVALID, "nq must be in [1, max_batch]");
+  if (e.quant != AES_QUANT_SYM_GLOBAL)
+    return aes::fail(AES_ERR_UNSUPPORTED, "pre-quantised queries take the symmetric B-bit values");
+  const int lo = -(1 << (e.bits - 1)), hi = (1 << (e.bits - 1)) - 1;
+  for (uint32_t i = 0; i < nq; i++) {
+    for (uint32_t c = 0; c < e.cols; c++) {
+      const int v = q[(size_t)i * e.cols + c];
+      if (v < lo || v > hi) return aes::fail(AES_ERR_QUERY, "query value outside the signed B-bit range");
+    }
+  }
+  cudaSetDevice(e.device);
+  std::memset(e.h_q8, 0, (size_t)nq * e.ld8);
+  for (uint32_t i = 0; i < nq; i++) std::memcpy(e.h_q8 + (size_t)i * e.ld8, q + (size_t)i * e.cols, e.cols);
+  AES_CK(cudaMemcpyAsync(e.d_q8, e.h_q8, (size_t)nq * e.ld8, cudaMemcpyHostToDevice, e.stream));
+  if (q_f32) {
+    for (uint32_t i = 0; i < nq; i++)
+      std::memcpy(e.h_q32 + (size_t)i * e.ld32, q_f32 + (size_t)i * e.cols, e.cols * 4ull);
+    AES_CK(cudaMemcpyAsync(e.d_q32, e.h_q32, (size_t)nq * e.ld32 * 4, cudaMemcpyHostToDevice, e.stream));
+  }
+  e.nq_loaded = nq;
+  e.q_pre = true;
+  e.q32_given = q_f32 != nullptr;
   return AES_OK;
 }
 
@@ -1167,11 +1243,13 @@ int aes_run(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score, uint
   if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
   cudaSetDevice(e.device);
   const uint32_t nq = e.nq_loaded;
-  e.last_q32 = e.d_q32;
+  const float* dq = e.q32_given ? e.d_q32 : nullptr;
+  e.last_q32 = dq;
+  e.last_int_final = e.int_final(dq);
   AES_CK(cudaEventRecord(e.ev0, e.stream));
   int rc = (e.prm.flags & AES_FLAG_GRAPHS)
-               ? e.enqueue_graph(e.d_q32, nq, k, e.d_out_idx, e.d_out_score, e.stream)
-               : e.enqueue(e.d_q32, nq, k, e.d_out_idx, e.d_out_score, e.stream);
+               ? e.enqueue_graph(dq, nq, k, e.d_out_idx, e.d_out_score, e.stream, e.q_pre)
+               : e.enqueue(dq, nq, k, e.d_out_idx, e.d_out_score, e.stream, e.q_pre);
   if (rc) return rc;
   AES_CK(cudaEventRecord(e.ev1, e.stream));
   uint32_t rep = 0;
@@ -1207,6 +1285,7 @@ int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t 
     d_queries = e.d_q32;
   }
   e.last_q32 = d_queries;
+  e.last_int_final = e.int_final(d_queries);
   int rc = (e.prm.flags & AES_FLAG_GRAPHS) ? e.enqueue_graph(d_queries, nq, k, d_idx, d_score, s)
                                            : e.enqueue(d_queries, nq, k, d_idx, d_score, s);
   if (rc) return rc;
@@ -1255,6 +1334,8 @@ int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score
   Engine& e = h->e;
   if (!e.nq_loaded) return aes::fail(AES_ERR_STATE, "aes_set_query must come first");
   if (k == 0 || k > e.prm.k_max) return aes::fail(AES_ERR_INVALID, "k must be in [1, k_max]");
+  if (!e.has_f32) return aes::fail(AES_ERR_STATE, "the matrix was created without FP32 values");
+  if (!e.q32_given) return aes::fail(AES_ERR_STATE, "the loaded queries have no FP32 values");
   AES_CK(cudaSetDevice(e.device));
   uint32_t kp = 1;
   while (kp < k) kp <<= 1;
@@ -1295,6 +1376,7 @@ int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score
   fa.out_idx = e.d_out_idx;
   fa.out_score = e.d_out_score;
   fa.status = nullptr;
+  fa.cand_key = nullptr;
   SelectArgs sa{};
   sa.q0 = 0;
   sa.split = 1;
@@ -1391,8 +1473,11 @@ int aes_read_candidates(aes_handle* h, uint32_t query, uint32_t* idx, int32_t* s
   AES_CK(cudaMemcpy(rows.data(), e.d_cand + (size_t)query * e.nslots, e.nslots * 4ull, cudaMemcpyDeviceToHost));
   AES_CK(cudaMemcpy(keys.data(), e.d_cand_key + (size_t)query * e.nslots, e.nslots * 4ull, cudaMemcpyDeviceToHost));
   std::vector<std::pair<uint32_t, uint32_t>> c;
+  // AES_FLAG_POSITIVE: Q_read_result's filter (host_spmv_ucsr.cpp:709) keeps scores above 0
+  // only; the integer key of score s is s ^ 2^31 and the FP32 key of x > 0 is above 2^31 as well
+  const bool positive = (e.prm.flags & AES_FLAG_POSITIVE) != 0;
   for (uint32_t i = 0; i < e.nslots; i++)
-    if (rows[i] != 0xFFFFFFFFu) c.emplace_back(keys[i], rows[i]);
+    if (rows[i] != 0xFFFFFFFFu && (!positive || keys[i] > 0x80000000u)) c.emplace_back(keys[i], rows[i]);
   std::sort(c.begin(), c.end(), [](const std::pair<uint32_t, uint32_t>& a,
                                    const std::pair<uint32_t, uint32_t>& b) {
     return a.first != b.first ? a.first > b.first : a.second > b.second;
@@ -1563,6 +1648,7 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
   fa.out_idx = d_idx;
   fa.out_score = d_score;
   fa.status = status;
+  fa.cand_key = e.has_f32 ? nullptr : cand_key;
   k_final<<<1, kThreadsFinal, e.final_smem, s>>>(fa);
   AES_CK(cudaGetLastError());
   uint32_t st = 0;

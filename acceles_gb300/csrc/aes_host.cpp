@@ -62,7 +62,7 @@ int check_csr(const uint64_t* ptr, const uint32_t* col, uint32_t rows, uint32_t 
 }
 
 int coo_to_csr(const uint32_t* row, const uint32_t* col, const float* val, uint32_t rows,
-               uint32_t cols, uint64_t nnz, HostCSR* out) {
+               uint32_t cols, uint64_t nnz, HostCSR* out, const int8_t* qval) {
   out->rows = rows;
   out->cols = cols;
   out->ptr.assign((size_t)rows + 1, 0);
@@ -73,30 +73,43 @@ int coo_to_csr(const uint32_t* row, const uint32_t* col, const float* val, uint3
   }
   for (uint32_t r = 0; r < rows; r++) out->ptr[r + 1] += out->ptr[r];
   out->col.resize(nnz);
-  out->val.resize(nnz);
+  out->val.resize(val ? nnz : 0);
+  out->qv.resize(qval ? nnz : 0);
   std::vector<uint64_t> pos(out->ptr.begin(), out->ptr.end() - 1);
   for (uint64_t i = 0; i < nnz; i++) {  // stable counting sort by row
     uint64_t d = pos[row[i]]++;
     out->col[d] = col[i];
-    out->val[d] = val[i];
+    if (val) out->val[d] = val[i];
+    if (qval) out->qv[d] = qval[i];
   }
   // stable sort by column inside each row (readMtx sorts tuples by (row, col), utils.hpp:331)
   parallel_for(rows, 4096, [&](uint64_t b, uint64_t e) {
-    std::vector<std::pair<uint32_t, float>> tmp;
+    std::vector<uint64_t> order;
+    std::vector<uint32_t> tc;
+    std::vector<float> tv;
+    std::vector<int8_t> tq;
     for (uint64_t r = b; r < e; r++) {
       uint64_t s = out->ptr[r], t = out->ptr[r + 1];
       bool sorted = true;
       for (uint64_t k = s + 1; k < t; k++)
         if (out->col[k] < out->col[k - 1]) { sorted = false; break; }
       if (sorted) continue;
-      tmp.clear();
-      for (uint64_t k = s; k < t; k++) tmp.emplace_back(out->col[k], out->val[k]);
-      std::stable_sort(tmp.begin(), tmp.end(),
-                       [](const std::pair<uint32_t, float>& a,
-                          const std::pair<uint32_t, float>& b2) { return a.first < b2.first; });
-      for (uint64_t k = s; k < t; k++) {
-        out->col[k] = tmp[k - s].first;
-        out->val[k] = tmp[k - s].second;
+      order.resize(t - s);
+      for (uint64_t k = s; k < t; k++) order[k - s] = k;
+      std::stable_sort(order.begin(), order.end(),
+                       [&](uint64_t x, uint64_t y) { return out->col[x] < out->col[y]; });
+      tc.resize(t - s);
+      for (uint64_t k = 0; k < t - s; k++) tc[k] = out->col[order[k]];
+      std::copy(tc.begin(), tc.end(), out->col.begin() + s);
+      if (val) {
+        tv.resize(t - s);
+        for (uint64_t k = 0; k < t - s; k++) tv[k] = out->val[order[k]];
+        std::copy(tv.begin(), tv.end(), out->val.begin() + s);
+      }
+      if (qval) {
+        tq.resize(t - s);
+        for (uint64_t k = 0; k < t - s; k++) tq[k] = out->qv[order[k]];
+        std::copy(tq.begin(), tq.end(), out->qv.begin() + s);
       }
     }
   });
@@ -226,10 +239,20 @@ int quantize_and_pack(const HostCSR& m, const aes_params& p, PackedMatrix* out) 
   out->quant = p.quant;
   out->P = (uint32_t)P;
 
+  const bool preq = m.prequantized;
+  if (preq && p.quant != AES_QUANT_SYM_GLOBAL)
+    return fail(AES_ERR_UNSUPPORTED, "pre-quantised matrices take the symmetric B-bit values");
+  if (preq) {
+    const int32_t lo = -(1 << (bits - 1)), hi = (1 << (bits - 1)) - 1;
+    for (uint64_t k = 0; k < nnz; k++)
+      if (m.qv[k] < lo || m.qv[k] > hi)
+        return fail(AES_ERR_INVALID, "pre-quantised value outside the signed B-bit range");
+  }
+
   // ---- scale ---------------------------------------------------------------------------------
   double gmax = 0.0;
   bool negative = false;
-  {
+  if (!preq) {
     unsigned nt = std::max(1u, std::thread::hardware_concurrency());
     std::vector<double> part(nt, 0.0);
     std::vector<char> neg(nt, 0);
@@ -268,6 +291,10 @@ int quantize_and_pack(const HostCSR& m, const aes_params& p, PackedMatrix* out) 
   parallel_for(rows, 1 << 14, [&](uint64_t b, uint64_t e) {
     for (uint64_t r = b; r < e; r++) {
       uint64_t s = m.ptr[r], t = m.ptr[r + 1];
+      if (preq) {  // every given entry is kept
+        qptr[r + 1] = t > s ? t - s : 1;
+        continue;
+      }
       double sc = gmax;
       if (per_row) {
         sc = 0.0;
@@ -290,6 +317,18 @@ int quantize_and_pack(const HostCSR& m, const aes_params& p, PackedMatrix* out) 
   parallel_for(rows, 1 << 14, [&](uint64_t b, uint64_t e) {
     for (uint64_t r = b; r < e; r++) {
       uint64_t s = m.ptr[r], t = m.ptr[r + 1];
+      if (preq) {
+        uint64_t o = qptr[r];
+        for (uint64_t k = s; k < t; k++, o++) {
+          qcol[o] = (uint16_t)m.col[k];
+          qval[o] = m.qv[k];
+        }
+        if (t == s) {  // a row without entries: one zero entry keeps the row flags aligned
+          qcol[o] = 0;
+          qval[o] = 0;
+        }
+        continue;
+      }
       double sc = gmax;
       if (per_row) {
         sc = 0.0;

@@ -29,12 +29,15 @@ struct HostCSR {
   uint32_t rows = 0, cols = 0;
   std::vector<uint64_t> ptr;  // rows + 1
   std::vector<uint32_t> col;
-  std::vector<float> val;
+  std::vector<float> val;     // FP32 values; empty for a pre-quantised matrix given without them
+  std::vector<int8_t> qv;     // pre-quantised B-bit values (the reference's q_val), or empty
+  bool prequantized = false;  // qv holds the values to pack (no quantiser)
 };
 
-// Stable (row, col) order; duplicates keep input order.
+// Stable (row, col) order; duplicates keep input order.  val and qval may each be null; the CSR
+// carries whichever arrays were given.
 int coo_to_csr(const uint32_t* row, const uint32_t* col, const float* val, uint32_t rows,
-               uint32_t cols, uint64_t nnz, HostCSR* out);
+               uint32_t cols, uint64_t nnz, HostCSR* out, const int8_t* qval = nullptr);
 int check_csr(const uint64_t* ptr, const uint32_t* col, uint32_t rows, uint32_t cols);
 
 // The quantised matrix in packed form, laid out for the device.
@@ -57,7 +60,10 @@ struct PackedMatrix {
 
 // Quantise (quantify_util.py:8-28 or the per-row variant), drop zero results
 // (matrix_to_coo), give rows left empty one entry (check_empty_rows, seeded), and pack the
-// result as Ultra-CSR in pack_parts row partitions (host_spmv_ucsr.cpp:278-425).
+// result as Ultra-CSR in pack_parts row partitions (host_spmv_ucsr.cpp:278-425).  A matrix with
+// pre-quantised values (m.prequantized) is packed as given, every entry kept (Q_packet_coo packs
+// the COO it is handed); a row without entries gets one entry of value 0 at column 0, so that
+// the row flags still count every row and its score stays 0.
 int quantize_and_pack(const HostCSR& m, const aes_params& p, PackedMatrix* out);
 
 // Reference-order packets (partition by partition, 64 bytes each) recovered from the tiled

@@ -38,14 +38,15 @@ GEN_FIXED_ABSNORMAL = 1
 GEN_GAMMA_DEG = 2
 GEN_FIXED_UNIFORM = 3
 
-EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_destroy", "aes_get_info",
-           "aes_set_query", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
+EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_create_quantized",
+           "aes_destroy", "aes_get_info", "aes_set_query", "aes_set_query_quantized", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
            "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_pack_tc_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact",
            "aes_retune", "aes_read_mtx", "aes_free", "aes_write_mtx", "aes_resparse"]
 
 FLAG_PROFILE = 1
 FLAG_GRAPHS = 2
 FLAG_TENSOR = 4  # 4-bit matrices: batched candidate pass on the tensor cores (tcgen05, FP8)
+FLAG_POSITIVE = 8  # read_candidates keeps scores above 0 only (Q_read_result's filter)
 
 
 class AesError(RuntimeError):
@@ -79,7 +80,7 @@ class Info(ctypes.Structure):
                 ("ck", ctypes.c_uint32), ("ck_effective", ctypes.c_uint32),
                 ("sample_tiles", ctypes.c_uint32), ("sample_rows", ctypes.c_uint32),
                 ("max_batch", ctypes.c_uint32), ("batch_tile", ctypes.c_uint32),
-                ("tensor_tiles", ctypes.c_uint32)]
+                ("tensor_tiles", ctypes.c_uint32), ("exact_pass", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -90,6 +91,7 @@ _u32p = ctypes.POINTER(ctypes.c_uint32)
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _f32p = ctypes.POINTER(ctypes.c_float)
+_i8p = ctypes.POINTER(ctypes.c_int8)
 
 
 def lib_path() -> str:
@@ -114,6 +116,12 @@ def load(build_if_missing: bool = True):
     L.aes_create_csr.restype = ctypes.c_int
     L.aes_create_csr.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                  ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_void_p)]
+    L.aes_create_quantized.restype = ctypes.c_int
+    L.aes_create_quantized.argtypes = [_u32p, _u32p, _i8p, _f32p, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(Params),
+                                       ctypes.POINTER(ctypes.c_void_p)]
+    L.aes_set_query_quantized.restype = ctypes.c_int
+    L.aes_set_query_quantized.argtypes = [ctypes.c_void_p, _i8p, _f32p, ctypes.c_uint32]
     L.aes_destroy.restype = ctypes.c_int
     L.aes_destroy.argtypes = [ctypes.c_void_p]
     L.aes_get_info.restype = ctypes.c_int
@@ -297,12 +305,28 @@ class SpMV:
     (host_spmv_ucsr.cpp:198-218), or from a sorted CSR with ``ptr=``.
     """
 
-    def __init__(self, rows, cols, row=None, col=None, val=None, ptr=None, **params):
+    def __init__(self, rows, cols, row=None, col=None, val=None, ptr=None, qval=None, **params):
+        """qval: the entries' pre-quantised B-bit values (int8) for the quantised constructor;
+        val may then be None (no FP32 exact pass)."""
         L = load()
         self._h = ctypes.c_void_p()
         self.params = default_params(**params)
         self.rows, self.cols = int(rows), int(cols)
-        if ptr is not None:
+        if qval is not None:
+            if ptr is not None:  # CSR given: expand to COO rows
+                ptr = np.asarray(ptr, np.uint64)
+                row = np.repeat(np.arange(self.rows, dtype=np.uint32), np.diff(ptr).astype(np.int64))
+            row = np.ascontiguousarray(row, np.uint32)
+            col = np.ascontiguousarray(col, np.uint32)
+            qv = np.ascontiguousarray(qval, np.int8)
+            vp = None
+            if val is not None:
+                val = np.ascontiguousarray(val, np.float32)
+                vp = _p(val, _f32p)
+            _check(L.aes_create_quantized(_p(row, _u32p), _p(col, _u32p), _p(qv, _i8p), vp,
+                                          self.rows, self.cols, row.shape[0],
+                                          ctypes.byref(self.params), ctypes.byref(self._h)))
+        elif ptr is not None:
             ptr = np.ascontiguousarray(ptr, np.uint64)
             col = np.ascontiguousarray(col, np.uint32)
             val = np.ascontiguousarray(val, np.float32)
@@ -327,6 +351,23 @@ class SpMV:
         if q.shape[1] != self.cols:
             raise ValueError("query length != cols")
         _check(load().aes_set_query(self._h, _p(q, _f32p), q.shape[0]))
+        self._nq = q.shape[0]
+        return 0
+
+    def Q_reset_quantized(self, qvec, q_f32=None):
+        """Load pre-quantised queries ([nq, cols] int8, the reference's q_type vector of
+        Q_reset, host_spmv_ucsr.cpp:790); q_f32 (optional) the same queries in FP32 for the
+        exact pass."""
+        q = np.ascontiguousarray(np.atleast_2d(qvec), np.int8)
+        if q.shape[1] != self.cols:
+            raise ValueError("query length != cols")
+        fp = None
+        if q_f32 is not None:
+            qf = np.ascontiguousarray(np.atleast_2d(q_f32), np.float32)
+            if qf.shape != q.shape:
+                raise ValueError("q_f32 shape != query shape")
+            fp = _p(qf, _f32p)
+        _check(load().aes_set_query_quantized(self._h, _p(q, _i8p), fp, q.shape[0]))
         self._nq = q.shape[0]
         return 0
 

@@ -71,6 +71,9 @@ typedef struct aes_params {
 #define AES_FLAG_GRAPHS 2u  /* replay each batch's launch sequence as a CUDA graph (captured once
                                per set of buffers, batch size and K); profiling events are
                                not recorded inside graphs */
+#define AES_FLAG_POSITIVE 8u /* aes_read_candidates returns only candidates whose score is above
+                               0, as Q_read_result keeps only positive slots
+                               (host_spmv_ucsr.cpp:709); the final Top-K is unaffected */
 #define AES_FLAG_TENSOR 4u  /* 4-bit matrices: lay the quantised entries out for the tensor
                                cores at creation (4 B per entry) and run the batched candidate
                                pass as FP8 tcgen05 products of 128-row tiles; the integers are
@@ -94,6 +97,8 @@ typedef struct aes_info {
   uint32_t split, ck, ck_effective, sample_tiles;
   uint32_t sample_rows, max_batch, batch_tile;
   uint32_t tensor_tiles;  /* 1 when the batched candidate pass runs on the tensor cores */
+  uint32_t exact_pass;    /* 1 when FP32 values are resident (the final Top-K is rescored in
+                             FP32); 0 for a pre-quantised matrix created without them */
 } aes_info;
 
 /* Defaults: bits 6, AES_QUANT_SYM_GLOBAL, AES_QQ_NUMPY, split 32, ck 512, k_max 100
@@ -108,6 +113,17 @@ void aes_params_default(aes_params* p);
  * ownership of its arrays. */
 int aes_create(const uint32_t* row, const uint32_t* col, const float* val, uint32_t rows,
                uint32_t cols, uint64_t nnz, const aes_params* p, aes_handle** out);
+/* The quantised constructor as the reference has it: SpMV(ConfigOpenCL&, q_x, q_y, q_val, rows,
+ * cols, nnz, q_vec, debug) (host_spmv_ucsr.cpp:198-218) with Q_packet_coo (:278) and Q_setup
+ * (:501).  q_val holds the B-bit signed values (the reference's ap_int<B> q_type) of a matrix
+ * quantised by the caller, e.g. from a _quantified_B*.mtx file (:969); p->quant must be
+ * AES_QUANT_SYM_GLOBAL and every value in [-2^(B-1), 2^(B-1) - 1] (else AES_ERR_INVALID).  The
+ * entries are packed as given (zeros included); a row without entries gets one zero entry.
+ * val (may be NULL) holds the entries' FP32 values for the exact pass: without them the final
+ * Top-K ranks the candidates by their integer score and aes_run_exact is unavailable. */
+int aes_create_quantized(const uint32_t* row, const uint32_t* col, const int8_t* q_val,
+                         const float* val, uint32_t rows, uint32_t cols, uint64_t nnz,
+                         const aes_params* p, aes_handle** out);
 /* Same from a CSR already sorted by (row, col): ptr[rows+1]. */
 int aes_create_csr(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
                    uint32_t cols, const aes_params* p, aes_handle** out);
@@ -128,6 +144,15 @@ int aes_retune(aes_handle* h, const aes_params* p);
  * (host_spmv_topk_csr_gpu_int8.cu:288); quantisation happens on the device. */
 int aes_set_query(aes_handle* h, const float* q, uint32_t nq);
 
+/* Load nq pre-quantised queries ([nq][cols] B-bit signed values, host memory) for the next
+ * aes_run: the candidate pass takes them as given, without the query quantiser.  Replaces
+ * Q_reset(q_type* vec, int debug) (host_spmv_ucsr.cpp:790-828) with the reference's quantised
+ * vector.  q_f32 (may be NULL) holds the same queries in FP32 for the exact pass; without it the
+ * final Top-K ranks the candidates by their integer score (out_score = that score).  The
+ * handle's quantiser must be AES_QUANT_SYM_GLOBAL; a value outside [-2^(B-1), 2^(B-1) - 1]
+ * returns AES_ERR_QUERY. */
+int aes_set_query_quantized(aes_handle* h, const int8_t* q, const float* q_f32, uint32_t nq);
+
 /* Run the loaded queries: candidate pass, Top-CK select, FP32 rescoring, Top-K.  out_idx and
  * out_score are host arrays [nq][k]; entries past the number of candidates are row
  * 0xFFFFFFFF with score -inf.  *ns (may be NULL) receives the device time in nanoseconds.
@@ -145,8 +170,9 @@ int aes_run_exact(aes_handle* h, uint32_t k, uint32_t* out_idx, float* out_score
 /* Candidates of query `query` of the last run in sort_tuples order (key descending, row
  * descending).  score_i32 gets the integer candidate score, key_f32 the ranking key (the
  * integer score, or rowscale * score under AES_QUANT_UNSIGNED_ROW); either may be NULL.
- * Replaces Q_read_result(res, idx, debug) (host_spmv_ucsr.cpp:691-748), which also drops
- * non-positive FPGA slots; every kept candidate is returned here. */
+ * Replaces Q_read_result(res, idx, debug) (host_spmv_ucsr.cpp:691-748).  With AES_FLAG_POSITIVE
+ * in the handle's flags only candidates scoring above 0 are returned, as the reference's
+ * `tmp_val > 0` (:709) keeps them; otherwise every candidate is. */
 int aes_read_candidates(aes_handle* h, uint32_t query, uint32_t* idx, int32_t* score_i32,
                         float* key_f32, uint32_t cap, uint32_t* n);
 

@@ -8,11 +8,14 @@
 //   long ns = q_spmv(true, debug);                               // :1099 (run, device ns)
 //   q_spmv.Q_read_result(res, idx, debug);                       // :1106 (merged candidates)
 //
-// Differences, by design: the constructor takes the FP32 COO (the engine quantises it and keeps
-// the FP32 copy for the exact pass) instead of a pre-quantised COO; the query is FP32 (the
-// engine quantises it on the device); errors throw aes::Error instead of exiting
-// (OCL_CHECK, opencl_utils.hpp:27-33); read_topk() adds the FP32-rescored final Top-K, which
-// the reference computes only in its Python scripts (quantify_util.py:332-372).
+// Two constructors: the reference's quantised one (pre-quantised COO values q_val and query q_vec,
+// as the reference's own main reads them from a _quantified_B*.mtx file, :969-977), and one taking
+// the FP32 COO, which the engine quantises itself and keeps for the exact pass.  Q_reset takes
+// either a quantised (int8) or an FP32 query.  The quantised constructor turns on Q_read_result's
+// filter of non-positive candidates (:709) unless params say otherwise.  Errors throw aes::Error
+// instead of exiting (OCL_CHECK, opencl_utils.hpp:27-33); read_topk() adds the final Top-K, FP32-
+// rescored when FP32 values are at hand, which the reference computes only in its Python scripts
+// (quantify_util.py:332-372).
 #pragma once
 
 #include <cstdint>
@@ -50,6 +53,24 @@ class SpMV {
     k_ = p.k_max;
     if (vec) Q_reset(vec, 0);
   }
+  // The quantised constructor SpMV(ConfigOpenCL&, q_x, q_y, q_val, rows, cols, nnz, q_vec,
+  // debug) (:198-218): q_val holds B-bit signed values, q_vec (may be null) the first quantised
+  // query; val_f32 (may be null) the FP32 values of the same entries for an exact pass.
+  SpMV(const uint32_t* q_x, const uint32_t* q_y, const int8_t* q_val, uint32_t rows,
+       uint32_t cols, uint64_t nnz, const int8_t* q_vec, int debug = 0,
+       const aes_params* params = nullptr, const float* val_f32 = nullptr)
+      : cols_(cols) {
+    (void)debug;
+    aes_params p;
+    if (params) p = *params;
+    else {
+      aes_params_default(&p);
+      p.flags |= AES_FLAG_POSITIVE;
+    }
+    check(aes_create_quantized(q_x, q_y, q_val, val_f32, rows, cols, nnz, &p, &h_));
+    k_ = p.k_max;
+    if (q_vec) Q_reset(q_vec, 0);
+  }
   SpMV(const SpMV&) = delete;
   SpMV& operator=(const SpMV&) = delete;
   SpMV(SpMV&& o) noexcept : h_(std::exchange(o.h_, nullptr)), cols_(o.cols_), k_(o.k_), nq_(o.nq_) {}
@@ -59,6 +80,15 @@ class SpMV {
   long Q_reset(const float* vec, int debug = 0, uint32_t nq = 1) {
     (void)debug;
     check(aes_set_query(h_, vec, nq));
+    nq_ = nq;
+    return 0;
+  }
+
+  // Q_reset(q_type* vec, int debug) (:790-828) with the reference's quantised query (or nq of
+  // them); q_f32 (may be null) the same queries in FP32 for the exact pass.
+  long Q_reset(const int8_t* vec, int debug = 0, uint32_t nq = 1, const float* q_f32 = nullptr) {
+    (void)debug;
+    check(aes_set_query_quantized(h_, vec, q_f32, nq));
     nq_ = nq;
     return 0;
   }
