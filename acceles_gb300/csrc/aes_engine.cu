@@ -340,6 +340,7 @@ int Engine::run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
   a.surv = d_surv;
   a.cap = cap;
   a.status = d_status;
+  a.mma_idle = (prm.flags & AES_FLAG_TEST_IDLE_MMA) ? 1u : 0u;
   const bool prof = (prm.flags & AES_FLAG_PROFILE) != 0;
   int rc = prof ? prof_open(s) : AES_OK;
   if (rc) return rc;
@@ -1651,11 +1652,18 @@ extern "C" int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, 
   fa.cand_key = e.has_f32 ? nullptr : cand_key;
   k_final<<<1, kThreadsFinal, e.final_smem, s>>>(fa);
   AES_CK(cudaGetLastError());
+  // counted like aes_run_device's launches: quantise, sample pass, threshold, filter pass,
+  // select, final
+  e.n_launch += 6;
+  e.n_cand += 1;
   uint32_t st = 0;
   AES_CK(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s));
   AES_CK(cudaStreamSynchronize(s));
   if (st & ST_QUERY) return aes::fail(AES_ERR_QUERY, "query has negative entries under an unsigned quantiser");
   if (st & (ST_MISS | ST_OVERFLOW)) {
+    e.n_launch += 3;
+    e.n_cand += 1;
+    e.n_repaired += 1;
     // exact slow path: every row's key into the handle's key array (reserved at creation),
     // each partition's Top-CK from it, then the FP32 rescoring
     if ((rc = plain(MODE_ALL, e.d_allkeys))) return rc;

@@ -72,6 +72,8 @@ struct TcArgs {
   uint2* surv;           // [nq_total][split][cap]
   uint32_t cap;
   uint32_t* status;      // [nq_total]
+  uint32_t mma_idle;     // failure-path test: the MMA role issues nothing, so every hand-over
+                         // wait of the other roles runs out and the CTA gives up
 };
 
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) {
@@ -83,6 +85,21 @@ __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) {
 __device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(2048u >> 4) << 16) |
          ((uint64_t)(128u >> 4) << 32) | ((uint64_t)1 << 46);
+}
+// Waits for the phase of the given parity to complete, for about a second at most, whether or
+// not another role has given up: the MMA thread's wait for its own MMAs in flight before the CTA
+// frees its tensor memory and leaves.
+__device__ __forceinline__ bool tc_wait_own(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  uint32_t done = 0;
+  while (!done) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (!done && clock64() - t0 > (1ll << 31)) return false;
+  }
+  return true;
 }
 // Waits for the phase of the given parity to complete.  Gives up after about a second, or as
 // soon as another thread of the CTA has given up (*gave_up set), so that every role leaves its
@@ -242,9 +259,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   float* thf = reinterpret_cast<float*>(sa + 2 * kTcChunkBytes);
   const uint32_t S = a.split <= 1 ? 1u : a.split;
   // mbarriers: staged[2] (producers -> MMA), mma_done[2] (MMA -> producers), acc_full[2]
-  // (MMA -> epilogue), acc_empty[2] (epilogue -> MMA)
+  // (MMA -> epilogue), acc_empty[2] (epilogue -> MMA), drain (the MMA thread's own MMAs done)
   uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * kTcQ);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
   volatile uint32_t* gave_up = tslot + 1;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   {
@@ -270,8 +287,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     }
   }
   if (tid == 0) {
-    for (int b = 0; b < 8; b++) {
-      const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers : (b >= 6 ? (uint32_t)kTcEpilogue : 1u);
+    for (int b = 0; b < 9; b++) {
+      const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers
+                                   : ((b >= 6 && b < 8) ? (uint32_t)kTcEpilogue : 1u);
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
     }
     *gave_up = 0u;
@@ -370,8 +388,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     // instruction descriptor: FP32 accumulator, e4m3 x e4m3, both K-major, N = 128, M = 128
     const uint32_t idesc = (1u << 4) | ((kTcQ >> 3) << 17) | ((kTcRows >> 4) << 24);
     const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
-    uint32_t tl = 0, c = 0;
-    for (uint32_t i = 0; i < total; i++) {
+    uint32_t tl = 0, c = 0, issued = 0;
+    for (uint32_t i = 0; i < total && !a.mma_idle; i++) {
       const uint32_t buf = i & 1u, d = tl & 1u;
       if (c == 0 && tl >= 2) ok &= tc_wait(b_empty + 8u * d, ((tl - 2) >> 1) & 1u, gave_up);
       if (ok) ok &= tc_wait(b_staged + 8u * buf, (i >> 1) & 1u, gave_up);
@@ -383,14 +401,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
                tc_desc(sq_addr + (c * 16u + 2u * kk) * 2048u), idesc, (c | kk) != 0);
       tc_commit(b_done + 8u * buf);
       if (c == a.nch - 1) tc_commit(b_full + 8u * d);
+      issued = i + 1;
       if (++c == a.nch) {
         c = 0;
         tl++;
       }
     }
-    // the last arrivals on the chunk barriers land before the CTA's shared memory goes away
-    if (ok && total >= 1) ok &= tc_wait(b_done + 8u * ((total - 1) & 1u), ((total - 1) >> 1) & 1u, gave_up);
-    if (ok && total >= 2) ok &= tc_wait(b_done + 8u * ((total - 2) & 1u), ((total - 2) >> 1) & 1u, gave_up);
+    // Before the CTA frees its tensor memory and its shared memory goes away, every MMA this
+    // thread issued has completed and the arrivals of its commits have landed, whether the
+    // roles finished or gave up: the last two chunk commits, the last tile commit, and a final
+    // commit on the drain barrier (each waited for at most about a second).
+    if (issued >= 1) {
+      bool drained = tc_wait_own(b_done + 8u * ((issued - 1) & 1u), ((issued - 1) >> 1) & 1u);
+      if (issued >= 2)
+        drained &= tc_wait_own(b_done + 8u * ((issued - 2) & 1u), ((issued - 2) >> 1) & 1u);
+      const uint32_t tiles_full = issued / a.nch;  // tiles whose accumulator commit was issued
+      if (tiles_full >= 1)
+        drained &= tc_wait_own(b_full + 8u * ((tiles_full - 1) & 1u), ((tiles_full - 1) >> 1) & 1u);
+      tc_commit(tc_smem_u32(bars + 8));
+      drained &= tc_wait_own(tc_smem_u32(bars + 8), 0u);
+      if (!drained) *gave_up = 1u;
+    }
   }
   tc_fence_before();
   __syncthreads();

@@ -47,6 +47,7 @@ FLAG_PROFILE = 1
 FLAG_GRAPHS = 2
 FLAG_TENSOR = 4  # 4-bit matrices: batched candidate pass on the tensor cores (tcgen05, FP8)
 FLAG_POSITIVE = 8  # read_candidates keeps scores above 0 only (Q_read_result's filter)
+FLAG_TEST_IDLE_MMA = 16  # failure-path tests: the tensor-core pass's waits run out
 
 
 class AesError(RuntimeError):

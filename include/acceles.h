@@ -81,6 +81,12 @@ typedef struct aes_params {
                                dp4a pass.  Ignored for 6- and 8-bit matrices, for matrices with
                                duplicate (row, col) entries and for split > 32 */
 
+#define AES_FLAG_TEST_IDLE_MMA 16u /* failure-path tests only: the tensor-core pass's MMA role
+                                     issues nothing, so the other roles' bounded waits run out
+                                     (about a second); the pass gives up, frees its tensor
+                                     memory and aes_run / aes_finish return AES_ERR_CUDA.  Has
+                                     no effect on the other passes */
+
 typedef struct aes_stats {
   uint64_t launches;       /* kernels launched by the engine since the last reset */
   uint64_t cand_launches;  /* full-matrix candidate-pass launches (the dominant kernel) */
@@ -189,9 +195,12 @@ int aes_run_device(aes_handle* h, const float* d_queries, uint32_t nq, uint32_t 
  * The per-query scratch (quantised query, sample keys, thresholds, survivors, candidates) is a
  * fixed 16 MiB device array inside the library instead; matrices whose scratch would not fit
  * are rejected with AES_ERR_UNSUPPORTED.  d_query [cols] FP32, d_idx / d_score [k] are device
- * pointers; `stream` a cudaStream_t (NULL = the handle's stream).  Synchronous.  The first call
- * on a device looks up the array's device address, so make that call before any stream capture.
- * All calls share the one array: calls that overlap on the GPU race and must not be issued. */
+ * pointers; `stream` a cudaStream_t (NULL = the handle's stream).  Synchronous: it waits for
+ * `stream` to read the query's status word before it returns (and, when the sample threshold
+ * missed, runs the exact slow path).  The first call on a device looks up the array's device
+ * address, so make that call before any stream capture.  All calls share the one array: calls
+ * that overlap on the GPU race and must not be issued.  Its launches and repairs count in
+ * aes_get_stats like those of aes_run_device. */
 int aes_run_noalloc(aes_handle* h, const float* d_query, uint32_t k, uint32_t* d_idx,
                     float* d_score, void* stream);
 

@@ -100,3 +100,27 @@ def test_tensor_layout_not_built_for_duplicates_or_wide_bits():
         e2 = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=bits, quant=1, split=1, ck=64,
                     k_max=10, max_batch=20, flags=E.FLAG_TENSOR)
         assert e2.info()["tensor_tiles"] == 0
+
+
+def test_tensor_pass_gives_up_and_recovers():
+    """The failure path of the pass's bounded waits: with the MMA role idle (a test flag) every
+    hand-over wait of the producers and the epilogue runs out after about a second, the pass
+    frees its tensor memory and the run returns AES_ERR_CUDA; the next ordinary run on the same
+    handle is oracle-exact, so the context and the tensor memory are usable again."""
+    rows, cols, k, ck, nq = 40000, 1024, 100, 256, 64  # 313 row tiles: every CTA has two or more
+    ptr, col, val = E.gen_matrix(E.GEN_UNIFORM_DEG, rows, cols, 10, 30, seed=77)
+    m = orc.Matrix(rows, cols, ptr, col, val, 4, orc.QUANT_UNSIGNED_ROW)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=E.QUANT_UNSIGNED_ROW,
+                 split=1, ck=ck, k_max=k, max_batch=nq, flags=E.FLAG_TENSOR)
+    assert eng.info()["tensor_tiles"] == 1
+    Q = queries(cols, nq, 78, signed=False)
+    eng.retune(flags=E.FLAG_TENSOR | E.FLAG_TEST_IDLE_MMA)
+    eng.Q_reset(Q)
+    with pytest.raises(E.AesError) as ex:
+        eng(k=k)
+    assert ex.value.code == E.AES_ERR_CUDA
+    eng.retune(flags=E.FLAG_TENSOR)
+    idx, sc, _ = run(eng, Q, k)
+    for i in (0, nq - 1):
+        oi, os_, _ = m.two_stage(Q[i], 1, ck, k)
+        assert np.array_equal(idx[i, :len(oi)], oi) and np.array_equal(sc[i, :len(oi)], os_)

@@ -55,3 +55,48 @@ def test_noalloc_rejects_scratch_over_limit():
     with pytest.raises(E.AesError) as ei:
         eng.run_noalloc(dq.data_ptr(), 10, oi.data_ptr(), os_.data_ptr())
     assert ei.value.code == E.AES_ERR_UNSUPPORTED
+
+
+def test_noalloc_exact_slow_path_matches_oracle():
+    # Scores decreasing with the row index put the global top rows in the first (sampled) tile,
+    # so the sample threshold admits too few rows and the entry point repairs the query on its
+    # exact slow path (every row's key, the select over all of them, the FP32 rescoring); two
+    # calls in a row, each checked against the oracle
+    import torch
+    import oracle as orc
+    rows, cols, k, ck = 40000, 256, 100, 512
+    ptr = np.arange(rows + 1, dtype=np.uint64) * 4
+    col = np.tile(np.array([0, 1, 2, 3], np.uint32), rows)
+    val = np.repeat(np.linspace(1.0, 0.01, rows).astype(np.float32), 4)
+    m = orc.Matrix(rows, cols, ptr, col, val, 8, orc.QUANT_SYM_GLOBAL)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=8, split=1, ck=ck, k_max=k,
+                 sample_stride=4)
+    q = np.ones(cols, np.float32)
+    oi_ref, os_ref, _ = m.two_stage(q, 1, ck, k)
+    dq = torch.from_numpy(q).cuda()
+    eng.stats(reset=True)
+    for _ in range(2):
+        oi = torch.full((k,), -1, dtype=torch.int32, device="cuda")
+        os_ = torch.zeros((k,), dtype=torch.float32, device="cuda")
+        eng.run_noalloc(dq.data_ptr(), k, oi.data_ptr(), os_.data_ptr())
+        torch.cuda.synchronize()
+        gi = oi.cpu().numpy().view(np.uint32)
+        gs = os_.cpu().numpy()
+        assert np.array_equal(gi[:len(oi_ref)], oi_ref)
+        assert np.allclose(gs[:len(os_ref)], os_ref, rtol=RTOL, atol=0)
+    st = eng.stats(reset=True)
+    assert st["repaired"] == 2 and st["cand_launches"] == 4 and st["launches"] >= 12
+
+
+def test_noalloc_rejects_negative_query_under_unsigned_quantiser():
+    import torch
+    rows, cols = 1000, 64
+    ptr, col, val = E.gen_matrix(E.GEN_UNIFORM_DEG, rows, cols, 2, 6, seed=1)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=8, quant=E.QUANT_UNSIGNED_ROW,
+                 split=1, ck=64, k_max=10)
+    dq = -torch.ones(cols, device="cuda")
+    oi = torch.empty(10, dtype=torch.int32, device="cuda")
+    os_ = torch.empty(10, dtype=torch.float32, device="cuda")
+    with pytest.raises(E.AesError) as ei:
+        eng.run_noalloc(dq.data_ptr(), 10, oi.data_ptr(), os_.data_ptr())
+    assert ei.value.code == E.AES_ERR_QUERY
