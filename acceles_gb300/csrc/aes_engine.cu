@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <tuple>
 #include <string>
@@ -89,6 +90,17 @@ static double binom_tail(uint32_t n, double f, uint32_t r) {
   }
   return s;
 }
+
+// Device arrays of a resident matrix (Ultra-CSR tiles, row bases, row scales, FP32 CSR,
+// tensor-core layout), shared by a handle and the views made from it: freed with the last of them.
+struct SharedAllocs {
+  int device = -1;
+  std::vector<void*> ptrs;
+  ~SharedAllocs() {
+    if (device >= 0) cudaSetDevice(device);
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
 
 struct Engine {
   aes_params prm{};
@@ -203,7 +215,8 @@ struct Engine {
   bool last_batched = false;
   std::vector<uint32_t> h_tile_rowbase;  // host copy: sample geometry is derived from it
   size_t bytes = 0, mat_bytes = 0, cfg_bytes = 0;
-  std::vector<void*> allocs, cfg_allocs;
+  std::vector<void*> allocs, cfg_allocs;  // this handle's own arrays
+  std::shared_ptr<SharedAllocs> mat_store;  // the matrix arrays, shared with views
 
   ~Engine() { release(); }
 
@@ -244,6 +257,7 @@ struct Engine {
     free_config();
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
+    mat_store.reset();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -268,6 +282,7 @@ struct Engine {
   }
 
   int build(const HostCSR& m, const aes_params& p);
+  int build_view(const Engine& base, const aes_params& p);
   int plan_config(const aes_params& p, Config* c) const;
   int apply_config(const Config& c);
   int retune(const aes_params& p);
@@ -663,6 +678,57 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     AES_CK(raise_smem((const void*)pick_batch((int)bits, sgn, mode)));
   AES_CK(raise_smem((const void*)k_final));
   if (tc_ready) AES_CK(raise_smem((const void*)k_cand_tc));
+  // the matrix arrays go to the store a view shares; the slow path's key array stays the handle's
+  mat_store = std::make_shared<SharedAllocs>();
+  mat_store->device = device;
+  std::vector<void*> own;
+  for (void* q : allocs) (q == (void*)d_allkeys ? own : mat_store->ptrs).push_back(q);
+  allocs.swap(own);
+  rc = apply_config(c);
+  if (rc) return rc;
+  AES_CK(cudaDeviceSynchronize());
+  return AES_OK;
+}
+
+// A view: another handle on base's resident matrix, with its own stream, slow-path key array and
+// per-batch buffers (configuration p), so that batches of one matrix run at the same time.
+int Engine::build_view(const Engine& b, const aes_params& p) {
+  if (p.bits != b.prm.bits || p.quant != b.prm.quant || p.pack_parts != b.prm.pack_parts ||
+      p.seed != b.prm.seed || p.device != b.prm.device)
+    return fail(AES_ERR_INVALID,
+                "bits, quant, pack_parts, seed and device are fixed by the packed matrix");
+  prm = p;
+  device = b.device;
+  AES_CK(cudaSetDevice(device));
+  sm_count = b.sm_count;
+  smem_optin = b.smem_optin;
+  AES_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  AES_CK(cudaEventCreate(&ev0));
+  AES_CK(cudaEventCreate(&ev1));
+  rows = b.rows; cols = b.cols; bits = b.bits; quant = b.quant; P = b.P;
+  nnz = b.nnz; qnnz = b.qnnz; packets = b.packets; tiles = b.tiles; sgn = b.sgn;
+  d_tiles = b.d_tiles; d_tile_rowbase = b.d_tile_rowbase; d_rowscale = b.d_rowscale;
+  d_tc_ptr = b.d_tc_ptr; d_tc_ent = b.d_tc_ent; tc_nch = b.tc_nch; tc_rtiles = b.tc_rtiles;
+  tc_ready = b.tc_ready;
+  d_csr_ptr = b.d_csr_ptr; d_csr_col = b.d_csr_col; d_csr_val = b.d_csr_val;
+  has_f32 = b.has_f32;
+  ld32 = b.ld32; ld8 = b.ld8;
+  h_tile_rowbase = b.h_tile_rowbase;
+  mat_store = b.mat_store;
+  Config c;
+  int rc = plan_config(p, &c);
+  if (rc) return rc;
+  const size_t plan = rows * 4ull + c.plan;
+  if (p.mem_limit && plan > p.mem_limit)
+    return fail(AES_ERR_NOMEM, "view needs " + std::to_string(plan) +
+                                   " device bytes, over the handle limit " +
+                                   std::to_string(p.mem_limit));
+  size_t freeb = 0, totalb = 0;
+  AES_CK(cudaMemGetInfo(&freeb, &totalb));
+  if (plan + (64ull << 20) > freeb)
+    return fail(AES_ERR_NOMEM, "view needs " + std::to_string(plan) + " device bytes, " +
+                                   std::to_string(freeb) + " free");
+  if ((rc = dalloc(&d_allkeys, rows)) != AES_OK) return rc;
   rc = apply_config(c);
   if (rc) return rc;
   AES_CK(cudaDeviceSynchronize());
@@ -1152,6 +1218,24 @@ int aes_pack_tc_host(const uint64_t* ptr, const uint32_t* col, const float* val,
     if (cap_entries < pm.tc_ent.size()) return aes::fail(AES_ERR_INVALID, "entry buffer too small");
     std::memcpy(entries, pm.tc_ent.data(), pm.tc_ent.size() * 4);
   }
+  return AES_OK;
+}
+
+int aes_create_view(const aes_handle* base, const aes_params* p, aes_handle** out) {
+  if (!base || !out) return aes::fail(AES_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  const aes_params prm = p ? *p : base->e.prm;
+  int rc = validate_params(&prm, base->e.rows, base->e.cols);
+  if (rc) return rc;
+  if (!base->e.mat_store) return aes::fail(AES_ERR_STATE, "the base handle holds no matrix");
+  aes_handle* h = new (std::nothrow) aes_handle();
+  if (!h) return aes::fail(AES_ERR_NOMEM, "host allocation failed");
+  rc = h->e.build_view(base->e, prm);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  *out = h;
   return AES_OK;
 }
 

@@ -39,7 +39,7 @@ GEN_GAMMA_DEG = 2
 GEN_FIXED_UNIFORM = 3
 
 EXPORTS = ["aes_params_default", "aes_create", "aes_create_csr", "aes_create_quantized",
-           "aes_destroy", "aes_get_info", "aes_set_query", "aes_set_query_quantized", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
+           "aes_create_view", "aes_destroy", "aes_get_info", "aes_set_query", "aes_set_query_quantized", "aes_run", "aes_read_candidates", "aes_run_device", "aes_finish",
            "aes_last_error", "aes_gen_matrix", "aes_pack_host", "aes_pack_tc_host", "aes_score_all", "aes_get_stats", "aes_run_noalloc", "aes_run_exact",
            "aes_retune", "aes_read_mtx", "aes_free", "aes_write_mtx", "aes_resparse"]
 
@@ -123,6 +123,9 @@ def load(build_if_missing: bool = True):
                                        ctypes.POINTER(ctypes.c_void_p)]
     L.aes_set_query_quantized.restype = ctypes.c_int
     L.aes_set_query_quantized.argtypes = [ctypes.c_void_p, _i8p, _f32p, ctypes.c_uint32]
+    L.aes_create_view.restype = ctypes.c_int
+    L.aes_create_view.argtypes = [ctypes.c_void_p, ctypes.POINTER(Params),
+                                  ctypes.POINTER(ctypes.c_void_p)]
     L.aes_destroy.restype = ctypes.c_int
     L.aes_destroy.argtypes = [ctypes.c_void_p]
     L.aes_get_info.restype = ctypes.c_int
@@ -306,14 +309,17 @@ class SpMV:
     (host_spmv_ucsr.cpp:198-218), or from a sorted CSR with ``ptr=``.
     """
 
-    def __init__(self, rows, cols, row=None, col=None, val=None, ptr=None, qval=None, **params):
+    def __init__(self, rows, cols, row=None, col=None, val=None, ptr=None, qval=None,
+                 _view_of=None, **params):
         """qval: the entries' pre-quantised B-bit values (int8) for the quantised constructor;
         val may then be None (no FP32 exact pass)."""
         L = load()
         self._h = ctypes.c_void_p()
         self.params = default_params(**params)
         self.rows, self.cols = int(rows), int(cols)
-        if qval is not None:
+        if _view_of is not None:
+            _check(L.aes_create_view(_view_of._h, ctypes.byref(self.params), ctypes.byref(self._h)))
+        elif qval is not None:
             if ptr is not None:  # CSR given: expand to COO rows
                 ptr = np.asarray(ptr, np.uint64)
                 row = np.repeat(np.arange(self.rows, dtype=np.uint32), np.diff(ptr).astype(np.int64))
@@ -425,6 +431,13 @@ class SpMV:
         _check(load().aes_run_noalloc(self._h, ctypes.c_void_p(d_query), k,
                                       ctypes.c_void_p(d_idx), ctypes.c_void_p(d_score),
                                       ctypes.c_void_p(stream) if stream else None))
+
+    def view(self, **changes):
+        """Another handle on this matrix (aes_create_view): its own stream and batch buffers, the
+        matrix shared; `changes` override this handle's parameters (ck, max_batch, flags, ...)."""
+        prm = {f: getattr(self.params, f) for f, _ in Params._fields_}
+        prm.update(changes)
+        return SpMV(self.rows, self.cols, _view_of=self, **prm)
 
     def retune(self, **changes):
         """Change ck, split, sample_stride, batch_tile, k_max, max_batch, flags, query_quant or

@@ -1,13 +1,16 @@
 """Serving loop: several device-resident matrices, continuous batching, admission by memory.
 
-Each matrix is one engine handle (its own CUDA stream) served by one worker thread.  A request
-(matrix, FP32 query, K) is queued on its matrix; a worker takes every request waiting when its
-previous batch completes (up to the handle's max_batch), runs them as one batch (from 16
-queries on, one matrix read scores 128 queries) and completes each request with its first K
-results.  Requests that arrive while a batch is on the GPU join the next batch as soon as the
-slot frees; batches of different matrices run on the GPU at the same time.  Matrices are
-admitted only if their device footprint fits the server's memory budget (the handle's
-mem_limit makes creation fail before allocating).
+Each matrix is resident once and has one or more batch slots: the engine handle that owns it and
+views of it (aes_create_view), each with its own CUDA stream and batch buffers, each served by
+one worker thread.  A request (matrix, FP32 query, K) is queued on its matrix; a free slot's
+worker takes every request waiting (up to max_batch), runs them as one batch (from 16 queries on,
+one matrix read scores 128 queries) and completes each request with its first K results.
+Requests that arrive while batches are on the GPU join the next batch as soon as a slot frees;
+batches of one matrix, and of different matrices, run on the GPU at the same time.
+
+Admission by device memory: a matrix is admitted only if the matrix and one batch slot fit the
+server's budget (the handle's mem_limit makes creation fail before allocating); each further
+slot is admitted only while its batch buffers still fit.
 
 Results do not depend on batching: each request's Top-K is the same alone and in any mix.
 
@@ -38,45 +41,66 @@ class _Request:
 
 
 class _Matrix:
-    def __init__(self, name, eng, cols, max_batch, k_max):
+    def __init__(self, name, engines, cols, max_batch, k_max):
         self.name = name
-        self.eng = eng
+        self.slots = engines  # the owning handle first, then its views
         self.cols = cols
         self.max_batch = max_batch
         self.k_max = k_max
         self.q = queue.Queue()
-        self.thread = None
+        self.threads = []
         self.batches = 0
         self.served = 0
+        self.lock = threading.Lock()
+        self.in_flight = 0      # batches of this matrix on the GPU now
+        self.max_in_flight = 0  # the most at once so far
 
 
 class Server:
     """Top-K SpMV server over device-resident matrices."""
 
-    def __init__(self, device: int = 0, mem_budget: int | None = None):
+    def __init__(self, device: int = 0, mem_budget: int | None = None, slots: int = 2):
         self.device = device
         self.mem_budget = mem_budget
+        self.slots = slots
         self.mem_used = 0
         self.mats: dict[str, _Matrix] = {}
         self.running = False
         self.lock = threading.Lock()
 
     # ---- admission ---------------------------------------------------------------------------
-    def add_matrix(self, name, rows, cols, ptr, col, val, max_batch=256, k_max=100, **params):
-        """Create a resident matrix; raises AesError(AES_ERR_NOMEM) if it does not fit."""
+    def _limit(self):
+        if self.mem_budget is None:
+            return 0
+        return max(1, self.mem_budget - self.mem_used)
+
+    def add_matrix(self, name, rows, cols, ptr, col, val, max_batch=256, k_max=100, slots=None,
+                   **params):
+        """Create a resident matrix with up to `slots` batch slots (the server's default if
+        None); raises AesError(AES_ERR_NOMEM) if the matrix and one slot do not fit.  Returns
+        the owning handle's info with the number of slots admitted."""
         with self.lock:
-            limit = 0
-            if self.mem_budget is not None:
-                limit = max(1, self.mem_budget - self.mem_used)
             eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, max_batch=max_batch,
-                         k_max=k_max, device=self.device, mem_limit=limit,
+                         k_max=k_max, device=self.device, mem_limit=self._limit(),
                          flags=params.pop("flags", E.FLAG_GRAPHS), **params)
             self.mem_used += eng.info()["device_bytes"]
-            m = _Matrix(name, eng, cols, max_batch, k_max)
+            engines = [eng]
+            for _ in range((slots or self.slots) - 1):
+                try:
+                    v = eng.view(mem_limit=self._limit())
+                except E.AesError as ex:
+                    if ex.code != E.AES_ERR_NOMEM:
+                        raise
+                    break  # the next slot's batch buffers do not fit the budget
+                self.mem_used += v.info()["device_bytes"]
+                engines.append(v)
+            m = _Matrix(name, engines, cols, max_batch, k_max)
             self.mats[name] = m
             if self.running:
-                self._start_worker(m)
-            return eng.info()
+                self._start_workers(m)
+            info = eng.info()
+            info["slots"] = len(engines)
+            return info
 
     # ---- requests ----------------------------------------------------------------------------
     def submit(self, name, query, k) -> Future:
@@ -91,22 +115,25 @@ class Server:
     def start(self):
         self.running = True
         for m in self.mats.values():
-            self._start_worker(m)
+            self._start_workers(m)
 
     def stop(self):
         self.running = False
         for m in self.mats.values():
-            m.q.put(None)
+            for _ in m.threads:
+                m.q.put(None)
         for m in self.mats.values():
-            if m.thread:
-                m.thread.join()
-                m.thread = None
+            for t in m.threads:
+                t.join()
+            m.threads = []
 
-    def _start_worker(self, m):
-        m.thread = threading.Thread(target=self._worker, args=(m,), daemon=True)
-        m.thread.start()
+    def _start_workers(self, m):
+        for eng in m.slots:
+            t = threading.Thread(target=self._worker, args=(m, eng), daemon=True)
+            t.start()
+            m.threads.append(t)
 
-    def _worker(self, m: _Matrix):
+    def _worker(self, m: _Matrix, eng):
         buf = np.zeros((m.max_batch, m.cols), np.float32)
         while True:
             first = m.q.get()
@@ -126,24 +153,32 @@ class Server:
             kmax = max(r.k for r in batch)
             for i, r in enumerate(batch):
                 buf[i] = r.query
+            with m.lock:
+                m.in_flight += 1
+                m.max_in_flight = max(m.max_in_flight, m.in_flight)
             try:
-                m.eng.Q_reset(buf[:n])
-                m.eng(k=kmax)
-                idx, sc = m.eng.read_topk()
+                eng.Q_reset(buf[:n])
+                eng(k=kmax)  # the GIL is released while the slot's stream runs
+                idx, sc = eng.read_topk()
             except Exception as ex:  # report the failure to every request of the batch
                 for r in batch:
                     r.future.set_exception(ex)
                 continue
+            finally:
+                with m.lock:
+                    m.in_flight -= 1
             t = time.perf_counter()
             for i, r in enumerate(batch):
                 r.future.set_result((idx[i, :r.k].copy(), sc[i, :r.k].copy(), t - r.t_submit))
-            m.batches += 1
-            m.served += n
+            with m.lock:
+                m.batches += 1
+                m.served += n
 
     def close(self):
         self.stop()
         for m in self.mats.values():
-            m.eng.close()
+            for eng in reversed(m.slots):
+                eng.close()
         self.mats.clear()
 
 
@@ -172,36 +207,45 @@ def run_load(server: Server, names, cols_of, rate, duration, ks=(8, 32, 100), se
     return len(futures) / (t_end - t0), float(np.percentile(lat, 50)), float(np.percentile(lat, 99)), len(futures)
 
 
+def serving_specs(scale=1):
+    """The three resident matrices of the serving workload: (name, generator, rows, cols, p0,
+    p1, seed); 1/scale of the rows for a small run."""
+    return [
+        ("1Mx900_12pct", E.GEN_FIXED_UNIFORM, 1_000_000 // scale, 900, 108, 0, 5101),
+        ("10Mx1024_deg20", E.GEN_UNIFORM_DEG, 10_000_000 // scale, 1024, 10, 30, 5102),
+        ("20Mx512_gamma32", E.GEN_GAMMA_DEG, 20_000_000 // scale, 512, 32, 512, 5103),
+    ]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rates", default="1000,10000,50000")
     ap.add_argument("--duration", type=float, default=5.0)
     ap.add_argument("--small", action="store_true", help="1/10 sized matrices")
     ap.add_argument("--max-batch", type=int, default=256)
+    ap.add_argument("--slots", type=int, default=2, help="batch slots per matrix")
     args = ap.parse_args()
     s = 10 if args.small else 1
-    specs = [  # name, kind, rows, cols, p0, p1
-        ("1Mx900_12pct", E.GEN_FIXED_UNIFORM, 1_000_000 // s, 900, 108, 0),
-        ("10Mx1024_deg20", E.GEN_UNIFORM_DEG, 10_000_000 // s, 1024, 10, 30),
-        ("20Mx512_gamma32", E.GEN_GAMMA_DEG, 20_000_000 // s, 512, 32, 512),
-    ]
-    srv = Server()
+    srv = Server(slots=args.slots)
     cols_of = {}
-    for name, kind, rows, cols, p0, p1 in specs:
-        ptr, col, val = E.gen_matrix(kind, rows, cols, p0, p1, seed=hash(name) & 0xFFFF)
+    for name, kind, rows, cols, p0, p1, seed in serving_specs(s):
+        ptr, col, val = E.gen_matrix(kind, rows, cols, p0, p1, seed=seed)
         info = srv.add_matrix(name, rows, cols, ptr, col, val, max_batch=args.max_batch,
-                              k_max=100, bits=8, split=1, ck=1024)
+                              k_max=100, bits=8, split=1, ck=1024, flags=0)
         cols_of[name] = cols
         print(json.dumps({"matrix": name, "rows": rows, "nnz": info["nnz"],
-                          "device_bytes": info["device_bytes"]}), flush=True)
+                          "device_bytes": info["device_bytes"], "slots": info["slots"]}),
+              flush=True)
     srv.start()
-    names = [sp[0] for sp in specs]
+    names = [sp[0] for sp in serving_specs(s)]
     run_load(srv, names, cols_of, 200, 1.0, seed=99)  # warm-up: graphs, caches
     for rate in [float(r) for r in args.rates.split(",")]:
         qps, p50, p99, n = run_load(srv, names, cols_of, rate, args.duration, seed=int(rate))
         print(json.dumps({"offered_qps": rate, "served_qps": qps, "p50_ms": p50 * 1e3,
                           "p99_ms": p99 * 1e3, "requests": n,
-                          "batches": {m.name: m.batches for m in srv.mats.values()}}), flush=True)
+                          "batches": {m.name: m.batches for m in srv.mats.values()},
+                          "max_in_flight": {m.name: m.max_in_flight for m in srv.mats.values()}}),
+              flush=True)
     srv.close()
 
 

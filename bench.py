@@ -402,6 +402,61 @@ def run_small(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+SERVE_METRIC = ("served queries/s with p50/p99 latency under Poisson arrivals, three resident "
+                "matrices (1Mx900 12%, 10Mx1024 deg 20, 20Mx512 gamma mean 32), 8-bit, K in {8,32,100}")
+
+
+def run_serve(args, rank, world):
+    """The serving workload: three device-resident 8-bit matrices, two batch slots each (the
+    handle and a view), Poisson arrivals at each offered rate for --serve-seconds, every request
+    picking a matrix and K uniformly.  `value` is the served rate at the highest offered rate."""
+    if rank != 0:
+        return
+    import torch
+    from acceles_gb300 import engine as E
+    from acceles_gb300 import serve as S
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    srv = S.Server(slots=2)
+    cols_of, mats = {}, []
+    for name, kind, rows, cols, p0, p1, seed in S.serving_specs():
+        ptr, col, val = E.gen_matrix(kind, rows, cols, p0, p1, seed=seed)
+        info = srv.add_matrix(name, rows, cols, ptr, col, val, max_batch=256, k_max=100, bits=8,
+                              split=1, ck=1024, flags=0)
+        cols_of[name] = cols
+        mats.append({"name": name, "rows": rows, "cols": cols, "nnz": info["nnz"],
+                     "slots": info["slots"], "device_bytes": info["device_bytes"]})
+        del ptr, col, val
+    srv.start()
+    names = list(cols_of)
+    for w in range(args.warmup):
+        S.run_load(srv, names, cols_of, 500, 0.5, seed=90 + w)
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    legs = []
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    for rate in rates:
+        qps, p50, p99, n = S.run_load(srv, names, cols_of, rate, args.serve_seconds, seed=int(rate))
+        legs.append({"offered_qps": rate, "served_qps": qps, "p50_ms": p50 * 1e3,
+                     "p99_ms": p99 * 1e3, "requests": n})
+    clk = clocks.stop()
+    in_flight = {m.name: m.max_in_flight for m in srv.mats.values()}
+    srv.close()
+    top = legs[-1]
+    line = {"metric": SERVE_METRIC, "value": top["served_qps"], "unit": "queries/s",
+            "n_gpus": 1, "steps": len(legs), "warmup": args.warmup,
+            "ms_per_step": args.serve_seconds * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded; reference matrices not shipped)",
+            "config": {"workload": "serving: 3 resident matrices, Poisson arrivals, K in {8,32,100}, "
+                                   "8-bit, CK=1024, split=1, max batch 256, 2 batch slots per matrix",
+                       "matrices": mats, "offered_rates": rates, "seconds_per_rate": args.serve_seconds},
+            "legs": legs, "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+            "max_batches_in_flight_per_matrix": in_flight, "clocks": clk,
+            "note": "a step is one offered rate held for seconds_per_rate; latency is submit to "
+                    "result on the host, queueing included"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,8 +477,12 @@ def main():
                     help="queries of one batched step checked against the oracle (spread over "
                          "the step); every query of one plain step is checked as well")
     ap.add_argument("--rows", type=int, default=ROWS, help="smaller matrix, for profiling only")
-    ap.add_argument("--workload", default="large", choices=["large", "small"],
-                    help="large: 10M x 1024 (the headline); small: the 400k x 500 plain-method case")
+    ap.add_argument("--workload", default="large", choices=["large", "small", "serve"],
+                    help="large: 10M x 1024 (the headline); small: the 400k x 500 plain-method "
+                         "case; serve: three resident matrices under Poisson arrivals")
+    ap.add_argument("--serve-rates", default="1000,10000,50000",
+                    help="offered queries/s of the serving workload")
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--split", type=int, default=1,
                     help="row partitions with a Top-(CK/split) each (the reference default is 32)")
     args = ap.parse_args()
@@ -439,6 +498,9 @@ def main():
         return
     if args.workload == "small":
         run_small(args, rank, world)
+        return
+    if args.workload == "serve":
+        run_serve(args, rank, world)
         return
 
     import torch

@@ -133,6 +133,15 @@ int aes_create_quantized(const uint32_t* row, const uint32_t* col, const int8_t*
 /* Same from a CSR already sorted by (row, col): ptr[rows+1]. */
 int aes_create_csr(const uint64_t* ptr, const uint32_t* col, const float* val, uint32_t rows,
                    uint32_t cols, const aes_params* p, aes_handle** out);
+/* A view: a second handle on the resident matrix of `base` (no copy of the matrix), with its own
+ * stream, per-batch buffers and configuration p (NULL: base's parameters; bits, quant,
+ * pack_parts, seed and device must equal base's).  Batches run on base and on its views at the
+ * same time, so a server keeps several batches of one matrix in flight.  The matrix arrays are
+ * freed with the last of the handle and its views; each is destroyed with aes_destroy, and each
+ * is used by one host thread at a time.  aes_info.device_bytes of a view counts only its own
+ * arrays.  No reference counterpart (the reference runs one query at a time, host_spmv_ucsr.cpp:
+ * 1084-1113). */
+int aes_create_view(const aes_handle* base, const aes_params* p, aes_handle** out);
 int aes_destroy(aes_handle* h);
 int aes_get_info(const aes_handle* h, aes_info* info);
 
