@@ -60,6 +60,28 @@ def metrics(idx, sc, exact, ks):
     return out
 
 
+def run_variant(ptr, col, val, rows, cols, Q, exact, bits, quant, split, ck, name=""):
+    """One candidate-pass variant at one CK: the engine's Top-max(KS) of every query in Q and its
+    metrics against the FP64 scores `exact` [nq, rows], with the candidate pass's GB/s."""
+    nq = Q.shape[0]
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=bits, quant=quant, split=split,
+                 ck=ck, k_max=max(KS), max_batch=nq, batch_tile=1, flags=E.FLAG_PROFILE)
+    try:
+        info = eng.info()
+        eng.Q_reset(Q)
+        eng.stats(reset=True)
+        eng(k=max(KS))
+        st = eng.stats(reset=True)
+        idx, sc = eng.read_topk()
+    finally:
+        eng.close()
+    launch_ms = st["cand_ms"] / max(st["cand_timed"], 1)
+    gbs = info["packet_bytes"] / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else None
+    return {"variant": name, "bits": bits, "ck": ck, "split": split,
+            "packet_bytes": info["packet_bytes"], "cand_pass_gbs": gbs,
+            "metrics": metrics(idx, sc, exact, KS)}, idx, sc
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rows", type=int, default=400_000)
@@ -85,23 +107,10 @@ def main():
                 ("B6 symmetric (reference default)", 6, E.QUANT_SYM_GLOBAL)]
     for name, bits, quant in variants:
         for ck in CKS:
-            eng = E.SpMV(args.rows, args.cols, ptr=ptr, col=col, val=val, bits=bits,
-                         quant=quant, split=args.split, ck=ck, k_max=max(KS), max_batch=nq,
-                         batch_tile=1, flags=E.FLAG_PROFILE)
-            info = eng.info()
-            eng.Q_reset(Q)
-            eng.stats(reset=True)
-            eng(k=max(KS))
-            st = eng.stats(reset=True)
-            idx, sc = eng.read_topk()
-            launch_ms = st["cand_ms"] / max(st["cand_timed"], 1)
-            gbs = info["packet_bytes"] / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else None
-            rec = {"variant": name, "bits": bits, "ck": ck, "split": args.split,
-                   "packet_bytes": info["packet_bytes"], "cand_pass_gbs": gbs,
-                   "metrics": metrics(idx, sc, exact, KS)}
+            rec, _, _ = run_variant(ptr, col, val, args.rows, args.cols, Q, exact, bits, quant,
+                                    args.split, ck, name)
             lines.append(rec)
             print(json.dumps(rec), flush=True)
-            eng.close()
     eng = E.SpMV(args.rows, args.cols, ptr=ptr, col=col, val=val, bits=8, split=1, ck=256,
                  k_max=max(KS), max_batch=nq)
     eng.Q_reset(Q)

@@ -127,3 +127,34 @@ def test_retune_drops_captured_graphs():
     fresh(k=k)
     fi, fs = fresh.read_topk()
     assert np.array_equal(idx, fi) and np.array_equal(sc, fs)
+
+
+def test_autotune_ck_equals_oracle_brute_force():
+    """The tuner's CK per split is the smallest of its ladder whose two-stage Top-K equals the
+    FP32 exact Top-K on every sample query, both computed here by the oracle alone; the chosen
+    pass is the fastest of the timed trials."""
+    from acceles_gb300 import autotune as AT
+    rows, cols, k, nq = 30000, 1024, 100, 20
+    ptr, col, val, m = _setup(rows, cols, bits=8, quant=0, seed=9)
+    eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=8, quant=0, split=1, ck=1024,
+                 k_max=k, max_batch=nq)
+    Q = _queries(cols, nq, 29)
+    ladder, splits = (64, 128, 256, 512, 1024), (1, 32)
+    res = AT.tune(eng, Q, k, ck_ladder=ladder, splits=splits, strides=(0, 16), reps=1,
+                  passes=((1, False), (128, False)))
+    xi, _ = orc.topk_f32_many(m.ptr, m.col, m.val, rows, cols, Q, k)
+    for split in splits:
+        want = None
+        for ck in ladder:
+            if ck < split:
+                continue
+            oi, _, on = orc.two_stage_many(m, Q, split, ck, k)
+            if all(np.array_equal(oi[i, :on[i]], xi[i, :on[i]]) and on[i] == k for i in range(nq)):
+                want = ck
+                break
+        got = [t["ck"] for t in res["ck_trials"] if t["split"] == split]
+        assert want is not None and got[-1] == want, (split, got, want)
+    best = min(res["time_trials"], key=lambda t: t["ms_per_query"])
+    assert res["params"]["ck"] == best["ck"] and res["params"]["split"] == best["split"]
+    assert res["params"]["batch_tile"] == best["batch_tile"]
+    assert res["params"]["sample_stride"] == best["sample_stride"]
