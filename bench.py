@@ -222,7 +222,7 @@ def make_queries(n, seed=SEED + 1):
 def headline_config(rows, nnz, split, batch):
     """The workload both arms report: identical dicts, so the two lines compare directly."""
     size = f"{rows // 1_000_000}M" if rows >= 1_000_000 else f"{rows // 1000}k"
-    return {"workload": f"{size}x1024 deg U{{10..30}} U(0,1), 8-bit Ultra-CSR, "
+    return {"workload": f"{size}x1024 deg U{{10..30}} U(0,1), {BITS}-bit Ultra-CSR, "
                         f"CK=1024, K=100, split={split}",
             "rows": rows, "cols": COLS, "nnz": int(nnz), "bits": BITS, "ck": CK,
             "split": split, "k": K, "batch": batch,
@@ -485,7 +485,12 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--split", type=int, default=1,
                     help="row partitions with a Top-(CK/split) each (the reference default is 32)")
+    ap.add_argument("--bits", type=int, default=8, choices=[4, 6, 8],
+                    help="bit width of the large workload (the headline is 8; the reference's "
+                         "default is 6)")
     args = ap.parse_args()
+    global BITS
+    BITS = args.bits
     args.warmup = max(args.warmup, 3)
     args.steps = max(1, args.steps)
 
@@ -617,13 +622,16 @@ def main():
     plain_alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + COLS
     plain_achieved = plain_alg / (plain_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic("cand_batch_10Mx1024_b8.md", "traffic_bytes_per_block")
+    # the committed ncu summaries are of the 8-bit, one-partition workload at 10M rows
+    profiled = BITS == 8 and args.split == 1 and rows == ROWS
+    traffic = (profile_traffic("cand_batch_10Mx1024_b8.md", "traffic_bytes_per_block")
+               if profiled else None)
     # the batched pass is bound by instruction issue, not HBM: warp instructions per group of
     # four entries (ncu instruction count of the capture) x the groups of one block, over the
     # live time per block at the sampled SM clock; an SM issues at most 4 warp instructions a cycle
     issue = None
     ipg = (profile_number("cand_batch_10Mx1024_b8.md", "warp_instructions_per_group")
-           if profile_current("cand_batch_10Mx1024_b8.md") else None)
+           if profiled and profile_current("cand_batch_10Mx1024_b8.md") else None)
     if ipg:
         groups = info["tiles"] * 32 * (511 // (BITS + 11)) // 4
         sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -635,7 +643,7 @@ def main():
                      "peak": 4.0, "frac": ach / 4.0, "instructions_per_block": ipl,
                      "instructions_per_group": ipg, "groups_per_block": groups,
                      "sm_mhz": mhz, "sms": sms}
-    plain_traffic = profile_traffic("cand_pass_10Mx1024_b8.md")
+    plain_traffic = profile_traffic("cand_pass_10Mx1024_b8.md") if profiled else None
 
     # end to end through the host-buffer C ABI (batched engine), same K steps
     eng.Q_reset(Qh[:B])
@@ -728,7 +736,7 @@ def main():
             "hbm_gbs_batched_pass": achieved, "hbm_gbs_plain_pass": plain_achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_cand_batch<8,signed,FILTER> (128 queries per matrix read)",
+                         "kernel": f"k_cand_batch<{BITS},signed,FILTER> (128 queries per matrix read)",
                          "limiter": "CUDA-core integer issue (gathers, byte transposes, dp4a); "
                                     "one matrix read serves 128 queries",
                          "alg_bytes_per_block": alg_bytes, "ms_per_block": cand_ms,
@@ -736,7 +744,7 @@ def main():
                          "issue": issue},
             "plain_roofline": {"bound": "hbm", "achieved": plain_achieved, "peak": peak,
                                "unit": "GB/s", "frac": plain_achieved / peak,
-                               "traffic": plain_traffic, "kernel": "k_cand_plain<8,signed,FILTER>",
+                               "traffic": plain_traffic, "kernel": f"k_cand_plain<{BITS},signed,FILTER>",
                                "alg_bytes_per_launch": plain_alg, "launch_ms": plain_launch_ms},
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": B * COLS * 4,
                     "d2h_bytes_per_step": B * K * 8},
