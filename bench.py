@@ -133,7 +133,9 @@ def tensor_4bit_leg(local, steps=5, warmup=3):
         # pass launches once per block, the dp4a pass once for every block)
         out[name] = {"queries_per_s": steps * nq / (ns / 1e9),
                      "ms_per_step": ns / 1e6 / steps,
-                     "pass_ms_per_128_queries": st["cand_ms"] / (nq // 128)}
+                     "pass_ms_per_128_queries": st["cand_ms"] / (nq // 128),
+                     "pass_launches_timed": int(st["cand_timed"]),
+                     "repaired_queries": int(st["repaired"])}
     # dense FP8 products of one launch: every 128-row tile times the 128-query operand
     flops = 2.0 * ((rows + 127) // 128) * 128 * 128 * 1024
     tc = out["tensor_cores"]
