@@ -41,7 +41,8 @@ constexpr int kTcEpiWarp = 8;
 constexpr int kTcEpilogue = 256;
 constexpr int kTcMmaWarp = 16;
 constexpr int kTcThreads = 17 * 32;
-constexpr uint32_t kTcTmemCols = 2 * kTcQ;  // two FP32 accumulators
+constexpr uint32_t kTcAcc = 4;  // FP32 accumulators in tensor memory
+constexpr uint32_t kTcTmemCols = kTcAcc * kTcQ;
 
 __host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split) {
   const uint32_t S = split <= 1 ? 1 : split;
@@ -158,51 +159,56 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 // Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, 64 queries) and
 // appends every (row, query) key at or above the query's threshold.  thf holds the thresholds as
 // FP32 bounds: the score (an exact integer in FP32) or rowscale * score is compared directly.
-// A block of 32 queries is compared without branches; only a block holding a hit (rare: the
-// thresholds pass about the Top-CK rows) takes the append path.
+// A block of 32 queries is compared without branches into a bit mask of hits.  The hits of a
+// thread then take their survivor slots with atomics issued back to back (none waits for
+// another's result) before any survivor is written, so a block costs one atomic round trip
+// however many of its queries hit; the eight epilogue warps all work on the same tile, so a
+// round trip per hit would leave nothing to hide it behind.
+// The thread's row of tile T, and its row scale (loaded before the accumulator wait, so that the
+// load's latency passes while the MMAs finish)
+__device__ __forceinline__ uint32_t tc_epi_row(uint32_t T) {
+  return T * kTcRows + ((threadIdx.x >> 5) & 3u) * 32u + (threadIdx.x & 31u);
+}
 __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_t tmem,
-                                            uint32_t dbuf, const float* thf_all, uint32_t S) {
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+                                            uint32_t dbuf, const float* thf_all, uint32_t S,
+                                            float rs) {
+  const uint32_t warp = threadIdx.x >> 5;
   const uint32_t g = warp & 3u, h = (warp - kTcEpiWarp) >> 2;
-  const uint32_t row = T * kTcRows + g * 32u + lane;
+  const uint32_t row = tc_epi_row(T);
   const bool valid = row < a.n_rows;
-  uint32_t p = 0;
-  float rs = 0.0f;
-  if (valid) {
-    p = part_of(row, S, a.slice);
-    if (a.rowscale) rs = __ldg(a.rowscale + row);
-  }
+  const uint32_t p = valid ? part_of(row, S, a.slice) : 0u;
   const float* thf = thf_all + p * kTcQ;
 #pragma unroll 1
   for (uint32_t col0 = h * 64u; col0 < h * 64u + 64u; col0 += 32u) {
     uint32_t v[32];
     tc_ld32(tmem + dbuf * kTcQ + col0 + ((g * 32u) << 16), v);
-    float t[32];  // the same 32 thresholds for every lane: 16-byte broadcast loads
+    uint32_t hit = 0;
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const float4 x = reinterpret_cast<const float4*>(thf + col0)[j];
-      t[4 * j] = x.x;
-      t[4 * j + 1] = x.y;
-      t[4 * j + 2] = x.z;
-      t[4 * j + 3] = x.w;
+    for (int j4 = 0; j4 < 8; j4++) {  // the same 32 thresholds for every lane: 16-byte broadcasts
+      const float4 x = reinterpret_cast<const float4*>(thf + col0)[j4];
+      const float tj[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float f = __uint_as_float(v[4 * j4 + u]);
+        hit |= ((a.rowscale ? __fmul_rn(f, rs) : f) >= tj[u] ? 1u : 0u) << (4 * j4 + u);
+      }
     }
-    bool any = false;
+    if (!valid || col0 >= a.nq) hit = 0;
+    else if (a.nq - col0 < 32u) hit &= (1u << (a.nq - col0)) - 1u;
+    const size_t qp0 = (size_t)(a.q0 + col0) * S + p;
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
-      const float f = __uint_as_float(v[j]);
-      any |= (a.rowscale ? __fmul_rn(f, rs) : f) >= t[j];
-    }
-    if (valid && any) {
+    for (int j0 = 0; j0 < 32; j0 += 16) {  // 16 slots at a time keeps the slot indices in registers
+      if (!((hit >> j0) & 0xFFFFu)) continue;
+      uint32_t ix[16];
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const uint32_t q = col0 + j;
-        const float f = __uint_as_float(v[j]);
-        const float x = a.rowscale ? __fmul_rn(f, rs) : f;
-        if (x >= t[j] && q < a.nq) {
-          const uint32_t key = a.rowscale ? key_f32(x) : key_i32(__float2int_rn(f));
-          const size_t qp = (size_t)(a.q0 + q) * S + p;
-          const uint32_t i = atomicAdd(a.cnt + qp, 1u);
-          if (i < a.cap) a.surv[qp * a.cap + i] = make_uint2(key, row);
+      for (int j = j0; j < j0 + 16; j++)
+        if ((hit >> j) & 1u) ix[j - j0] = atomicAdd(a.cnt + qp0 + (size_t)j * S, 1u);
+#pragma unroll
+      for (int j = j0; j < j0 + 16; j++) {
+        if (((hit >> j) & 1u) && ix[j - j0] < a.cap) {
+          const float f = __uint_as_float(v[j]);
+          const uint32_t key = a.rowscale ? key_f32(__fmul_rn(f, rs)) : key_i32(__float2int_rn(f));
+          a.surv[(qp0 + (size_t)j * S) * a.cap + ix[j - j0]] = make_uint2(key, row);
         }
       }
     }
@@ -261,7 +267,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   // mbarriers: staged[2] (producers -> MMA), mma_done[2] (MMA -> producers), acc_full[2]
   // (MMA -> epilogue), acc_empty[2] (epilogue -> MMA), drain (the MMA thread's own MMAs done)
   uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * kTcQ);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5 + 2 * kTcAcc);
   volatile uint32_t* gave_up = tslot + 1;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   {
@@ -287,9 +293,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     }
   }
   if (tid == 0) {
-    for (int b = 0; b < 9; b++) {
+    for (int b = 0; b < 5 + 2 * (int)kTcAcc; b++) {
       const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers
-                                   : ((b >= 6 && b < 8) ? (uint32_t)kTcEpilogue : 1u);
+                                   : ((b >= 4 + (int)kTcAcc && b < 4 + 2 * (int)kTcAcc) ? (uint32_t)kTcEpilogue : 1u);
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
     }
     *gave_up = 0u;
@@ -306,7 +312,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = *tslot;
   const uint32_t b_staged = tc_smem_u32(bars), b_done = tc_smem_u32(bars + 2);
-  const uint32_t b_full = tc_smem_u32(bars + 4), b_empty = tc_smem_u32(bars + 6);
+  const uint32_t b_full = tc_smem_u32(bars + 4), b_empty = tc_smem_u32(bars + 4 + kTcAcc);
   const uint32_t ntl = a.n_rtiles > blockIdx.x ? (a.n_rtiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
   const uint32_t total = ntl * a.nch;  // chunks of this CTA
   bool ok = true;
@@ -374,12 +380,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   } else if (warp < kTcEpiWarp + kTcEpilogue / 32) {
     // ---- epilogue -----------------------------------------------------------------------------
     for (uint32_t tl = 0; tl < ntl; tl++) {
-      const uint32_t d = tl & 1u;
-      ok &= tc_wait(b_full + 8u * d, (tl >> 1) & 1u, gave_up);
+      const uint32_t d = tl % kTcAcc;
+      const uint32_t T = blockIdx.x + tl * gridDim.x, row = tc_epi_row(T);
+      const float rs = (a.rowscale && row < a.n_rows) ? __ldg(a.rowscale + row) : 0.0f;
+      ok &= tc_wait(b_full + 8u * d, (tl / kTcAcc) & 1u, gave_up);
       ok = __all_sync(0xFFFFFFFFu, ok);  // tcgen05.ld needs the whole warp
       if (!ok) break;
       tc_fence_after();
-      tc_epilogue(a, blockIdx.x + tl * gridDim.x, tmem, d, thf, S);
+      tc_epilogue(a, T, tmem, d, thf, S, rs);
       tc_fence_before();
       tc_arrive(b_empty + 8u * d);
     }
@@ -390,8 +398,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
     uint32_t tl = 0, c = 0, issued = 0;
     for (uint32_t i = 0; i < total && !a.mma_idle; i++) {
-      const uint32_t buf = i & 1u, d = tl & 1u;
-      if (c == 0 && tl >= 2) ok &= tc_wait(b_empty + 8u * d, ((tl - 2) >> 1) & 1u, gave_up);
+      const uint32_t buf = i & 1u, d = tl % kTcAcc;
+      if (c == 0 && tl >= kTcAcc) ok &= tc_wait(b_empty + 8u * d, ((tl - kTcAcc) / kTcAcc) & 1u, gave_up);
       if (ok) ok &= tc_wait(b_staged + 8u * buf, (i >> 1) & 1u, gave_up);
       if (!ok) break;
       tc_fence_after();
@@ -416,10 +424,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
       if (issued >= 2)
         drained &= tc_wait_own(b_done + 8u * ((issued - 2) & 1u), ((issued - 2) >> 1) & 1u);
       const uint32_t tiles_full = issued / a.nch;  // tiles whose accumulator commit was issued
-      if (tiles_full >= 1)
-        drained &= tc_wait_own(b_full + 8u * ((tiles_full - 1) & 1u), ((tiles_full - 1) >> 1) & 1u);
-      tc_commit(tc_smem_u32(bars + 8));
-      drained &= tc_wait_own(tc_smem_u32(bars + 8), 0u);
+      for (uint32_t j = 1; j <= kTcAcc && j <= tiles_full; j++)  // the last use of each accumulator
+        drained &= tc_wait_own(b_full + 8u * ((tiles_full - j) % kTcAcc), ((tiles_full - j) / kTcAcc) & 1u);
+      tc_commit(tc_smem_u32(bars + 4 + 2 * kTcAcc));
+      drained &= tc_wait_own(tc_smem_u32(bars + 4 + 2 * kTcAcc), 0u);
       if (!drained) *gave_up = 1u;
     }
   }
