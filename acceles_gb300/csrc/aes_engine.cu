@@ -212,6 +212,7 @@ struct Engine {
   uint8_t* d_qtab_tc = nullptr;   // [blocks][tc_qtab_bytes(cols)] e4m3 query operands
   size_t tc_smem = 0;
   int tc_grid = 0;
+  uint32_t tc_nb = 2;  // chunk buffers of the tensor-core pass (tc_bufs)
   bool last_batched = false;
   std::vector<uint32_t> h_tile_rowbase;  // host copy: sample geometry is derived from it
   size_t bytes = 0, mat_bytes = 0, cfg_bytes = 0;
@@ -306,7 +307,7 @@ struct Engine {
   // every partition in shared memory, batched passes allowed
   bool tc_usable(const aes_params& p, uint32_t S) const {
     return tc_ready && (p.flags & AES_FLAG_TENSOR) && S <= kTcMaxSplit && p.batch_tile != 1 &&
-           tc_smem_bytes(cols, S) <= (size_t)smem_optin;
+           tc_smem_bytes(cols, S, 2) <= (size_t)smem_optin;
   }
 };
 
@@ -359,7 +360,10 @@ int Engine::run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
   const bool prof = (prm.flags & AES_FLAG_PROFILE) != 0;
   int rc = prof ? prof_open(s) : AES_OK;
   if (rc) return rc;
-  k_cand_tc<<<tc_grid, kTcThreads, tc_smem, s>>>(a);
+  if (tc_nb == 3)
+    k_cand_tc<3><<<tc_grid, kTcThreads, tc_smem, s>>>(a);
+  else
+    k_cand_tc<2><<<tc_grid, kTcThreads, tc_smem, s>>>(a);
   AES_CK(cudaGetLastError());
   if (prof && (rc = prof_close(s))) return rc;
   n_launch++;
@@ -554,7 +558,8 @@ int Engine::apply_config(const Config& c) {
     batch_grid = std::max(1, occb) * sm_count;
   }
   if (use_tc) {  // one CTA per SM (its shared memory), persistent over the 128-row tiles
-    tc_smem = tc_smem_bytes(cols, split);
+    tc_nb = tc_bufs(cols, split, (size_t)smem_optin);
+    tc_smem = tc_smem_bytes(cols, split, tc_nb);
     tc_grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)sm_count, tc_rtiles));
   } else {
     d_qtab_tc = nullptr;
@@ -681,7 +686,10 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
   for (int mode = 0; mode < 2; mode++)
     AES_CK(raise_smem((const void*)pick_batch((int)bits, sgn, mode)));
   AES_CK(raise_smem((const void*)k_final));
-  if (tc_ready) AES_CK(raise_smem((const void*)k_cand_tc));
+  if (tc_ready) {
+    AES_CK(raise_smem((const void*)k_cand_tc<2>));
+    AES_CK(raise_smem((const void*)k_cand_tc<3>));
+  }
   // the matrix arrays go to the store a view shares; the slow path's key array stays the handle's
   mat_store = std::make_shared<SharedAllocs>();
   mat_store->device = device;

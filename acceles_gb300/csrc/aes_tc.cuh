@@ -43,10 +43,21 @@ constexpr int kTcMmaWarp = 16;
 constexpr int kTcThreads = 17 * 32;
 constexpr uint32_t kTcAcc = 4;  // FP32 accumulators in tensor memory
 constexpr uint32_t kTcTmemCols = kTcAcc * kTcQ;
+// mbarriers of a kernel with NB chunk buffers: staged[NB] (producers -> MMA), done[NB] (MMA ->
+// producers), full[kTcAcc] (MMA -> epilogue), empty[kTcAcc] (epilogue -> MMA), drain (the MMA
+// thread's own MMAs complete); then the tensor-memory address and the give-up flag
+__host__ __device__ constexpr uint32_t tc_nbars(uint32_t nb) { return 2 * nb + 2 * kTcAcc + 1; }
 
-__host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split) {
+// shared memory of the pass with nb chunk buffers (2 or 3)
+__host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split, uint32_t nb) {
   const uint32_t S = split <= 1 ? 1 : split;
-  return tc_qtab_bytes(cols) + 2 * (size_t)kTcChunkBytes + (size_t)S * kTcQ * 4 + 128;
+  return tc_qtab_bytes(cols) + nb * (size_t)kTcChunkBytes + (size_t)S * kTcQ * 4 +
+         ((tc_nbars(nb) * 8 + 8 + 15) & ~15u);
+}
+// chunk buffers for a configuration: three where they fit next to the query operand and the
+// thresholds (the producers then run two chunks ahead of the MMAs), else two
+__host__ inline uint32_t tc_bufs(uint32_t cols, uint32_t split, size_t smem_limit) {
+  return tc_smem_bytes(cols, split, 3) <= smem_limit ? 3u : 2u;
 }
 
 // e4m3 query operand of queries q0 .. q0 + nq - 1 (zero past nq and past cols)
@@ -256,18 +267,21 @@ __device__ __forceinline__ bool tc_producers_any(bool fail) {
 }
 
 // One CTA per SM, persistent over row tiles T = blockIdx.x, + gridDim.x, ...  Chunk i of the CTA
-// is chunk i % nch of its tile i / nch; chunk buffer i & 1; accumulator (tile t) t & 1.
+// is chunk i % nch of its tile i / nch; chunk buffer i % NB; accumulator (tile t) t % kTcAcc.
+template <uint32_t NB>
 __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
+  static_assert(NB == 2 || NB == 3, "two or three chunk buffers");
+  constexpr uint32_t kDone = NB, kFull = 2 * NB, kEmpty = 2 * NB + kTcAcc;
+  constexpr uint32_t kDrain = kEmpty + kTcAcc, kBars = tc_nbars(NB);
+  constexpr uint32_t R = NB + 2;  // producer ring: the chunks of every buffer and two ahead
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t qbytes = (a.kpad / 16u) * 2048u;
   unsigned char* sq = smem;                     // query operand
-  unsigned char* sa = smem + qbytes;            // two chunk buffers of the row tile
-  float* thf = reinterpret_cast<float*>(sa + 2 * kTcChunkBytes);
+  unsigned char* sa = smem + qbytes;            // NB chunk buffers of the row tile
+  float* thf = reinterpret_cast<float*>(sa + NB * kTcChunkBytes);
   const uint32_t S = a.split <= 1 ? 1u : a.split;
-  // mbarriers: staged[2] (producers -> MMA), mma_done[2] (MMA -> producers), acc_full[2]
-  // (MMA -> epilogue), acc_empty[2] (epilogue -> MMA), drain (the MMA thread's own MMAs done)
   uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * kTcQ);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5 + 2 * kTcAcc);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kBars);
   volatile uint32_t* gave_up = tslot + 1;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   {
@@ -275,7 +289,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     uint4* dst = reinterpret_cast<uint4*>(sq);
     for (uint32_t i = tid; i < qbytes / 16u; i += blockDim.x) dst[i] = src[i];
     uint4* z = reinterpret_cast<uint4*>(sa);
-    for (uint32_t i = tid; i < 2 * kTcChunkBytes / 16u; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    for (uint32_t i = tid; i < NB * kTcChunkBytes / 16u; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
     // thresholds as FP32 bounds on the score (int keys) or on rowscale * score:
     // key >= th  <=>  x >= bound for every x the pass produces
     for (uint32_t i = tid; i < S * kTcQ; i += blockDim.x) {
@@ -293,9 +307,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     }
   }
   if (tid == 0) {
-    for (int b = 0; b < 5 + 2 * (int)kTcAcc; b++) {
-      const uint32_t cnt = (b < 2) ? (uint32_t)kTcProducers
-                                   : ((b >= 4 + (int)kTcAcc && b < 4 + 2 * (int)kTcAcc) ? (uint32_t)kTcEpilogue : 1u);
+    for (uint32_t b = 0; b < kBars; b++) {
+      const uint32_t cnt = (b < kDone) ? (uint32_t)kTcProducers
+                                       : ((b >= kEmpty && b < kDrain) ? (uint32_t)kTcEpilogue : 1u);
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
     }
     *gave_up = 0u;
@@ -311,18 +325,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t b_staged = tc_smem_u32(bars), b_done = tc_smem_u32(bars + 2);
-  const uint32_t b_full = tc_smem_u32(bars + 4), b_empty = tc_smem_u32(bars + 4 + kTcAcc);
+  const uint32_t b_staged = tc_smem_u32(bars), b_done = tc_smem_u32(bars + kDone);
+  const uint32_t b_full = tc_smem_u32(bars + kFull), b_empty = tc_smem_u32(bars + kEmpty);
   const uint32_t ntl = a.n_rtiles > blockIdx.x ? (a.n_rtiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
   const uint32_t total = ntl * a.nch;  // chunks of this CTA
   bool ok = true;
 
   if (warp < kTcProducers / 32) {
     // ---- producers ----------------------------------------------------------------------------
-    // Chunk i lives in ring set E[i % 4] (static names: the step is dispatched four ways).  Step i
-    // clears chunk i - 2 from E[(i + 2) % 4], loads chunk i + 2 into it and stages chunk i
-    // (loaded two steps earlier); row offsets are read four steps before the entries.  So no
-    // register a store or a copy reads waits on a load in flight.
+    // Chunk i lives in ring set E[i % R], R = NB + 2 (indices fixed at compile time: the loop
+    // below is unrolled R ways).  Step i clears chunk i - NB, the last chunk of buffer i % NB,
+    // from E[(i + 2) % R], loads chunk i + 2 into that set and stages chunk i (loaded two steps
+    // earlier); a chunk's row offsets are read R steps before its entries.  So no register a
+    // store or a copy reads waits on a load in flight.
     // chunk id of chunk i: tile blockIdx.x + (i / nch) gridDim.x, chunk i % nch; kept
     // incrementally for the look-ahead chunk (no division per step)
     uint32_t la_i = 0, la_t = blockIdx.x, la_c = 0;
@@ -337,45 +352,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
         la_t += gridDim.x;
       }
     };
-    TcEnt E0, E1, E2, E3;
-    uint32_t P0b, P0e, P1b, P1e, P2b, P2e, P3b, P3e;  // row offsets of chunk i + 2 in P[(i + 2) % 4]
+    TcEnt E[R];
+    uint32_t Pb[R], Pe[R];  // P[j % R]: row offsets of chunk j, for j = i + 2 .. i + R + 1
     {
       uint32_t b, e;
       ptr_next(b, e);
-      E0.load(a.ent, b, e - b, tid);
+      E[0].load(a.ent, b, e - b, tid);
       ptr_next(b, e);
-      E1.load(a.ent, b, e - b, tid);
-      ptr_next(P2b, P2e);
-      ptr_next(P3b, P3e);
-      ptr_next(P0b, P0e);
-      ptr_next(P1b, P1e);
+      E[1].load(a.ent, b, e - b, tid);
+#pragma unroll
+      for (uint32_t j = 2; j < R + 2; j++) ptr_next(Pb[j % R], Pe[j % R]);
     }
+    uint32_t buf = 0;  // i % NB
     auto step = [&](uint32_t i, TcEnt& cur, TcEnt& old, uint32_t& pb, uint32_t& pe) -> bool {
-      const uint32_t buf = i & 1u;
       unsigned char* ab = sa + buf * kTcChunkBytes;
-      if (i >= 2) {  // the MMAs of chunk i - 2 have read this buffer: clear its entries
-        ok &= tc_wait(b_done + 8u * buf, ((i - 2) >> 1) & 1u, gave_up);
+      if (i >= NB) {  // the MMAs of chunk i - NB have read this buffer: clear its entries
+        ok &= tc_wait(b_done + 8u * buf, ((i - NB) / NB) & 1u, gave_up);
         if (ok) old.stage(ab, a.ent, tid, true);
       }
       // every clear lands before any write of this chunk (they may share a byte); the
       // producers leave together at the first failure
       if (tc_producers_any(!ok)) return false;
       old.load(a.ent, pb, pe - pb, tid);  // chunk i + 2
-      ptr_next(pb, pe);                   // chunk i + 6
+      ptr_next(pb, pe);                   // chunk i + R + 2
       cur.stage(ab, a.ent, tid, false);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tc_arrive(b_staged + 8u * buf);
+      buf = buf + 1 == NB ? 0u : buf + 1;
       return true;
     };
-    for (uint32_t i = 0; i < total; i++) {
-      bool go;
-      switch (i & 3u) {
-        case 0: go = step(i, E0, E2, P2b, P2e); break;
-        case 1: go = step(i, E1, E3, P3b, P3e); break;
-        case 2: go = step(i, E2, E0, P0b, P0e); break;
-        default: go = step(i, E3, E1, P1b, P1e); break;
+    bool go = true;
+    for (uint32_t i0 = 0; go && i0 < total; i0 += R) {
+#pragma unroll
+      for (uint32_t k = 0; k < R; k++) {
+        if (i0 + k >= total) break;
+        go = step(i0 + k, E[k], E[(k + 2) % R], Pb[(k + 2) % R], Pe[(k + 2) % R]);
+        if (!go) break;
       }
-      if (!go) break;
     }
   } else if (warp < kTcEpiWarp + kTcEpilogue / 32) {
     // ---- epilogue -----------------------------------------------------------------------------
@@ -398,9 +411,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
     uint32_t tl = 0, c = 0, issued = 0;
     for (uint32_t i = 0; i < total && !a.mma_idle; i++) {
-      const uint32_t buf = i & 1u, d = tl % kTcAcc;
+      const uint32_t buf = i % NB, d = tl % kTcAcc;
       if (c == 0 && tl >= kTcAcc) ok &= tc_wait(b_empty + 8u * d, ((tl - kTcAcc) / kTcAcc) & 1u, gave_up);
-      if (ok) ok &= tc_wait(b_staged + 8u * buf, (i >> 1) & 1u, gave_up);
+      if (ok) ok &= tc_wait(b_staged + 8u * buf, (i / NB) & 1u, gave_up);
       if (!ok) break;
       tc_fence_after();
       const uint32_t nk = min(kTcChunkK, a.kpad - c * kTcChunkK) / 32u;
@@ -417,17 +430,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     }
     // Before the CTA frees its tensor memory and its shared memory goes away, every MMA this
     // thread issued has completed and the arrivals of its commits have landed, whether the
-    // roles finished or gave up: the last two chunk commits, the last tile commit, and a final
-    // commit on the drain barrier (each waited for at most about a second).
+    // roles finished or gave up: the last commit of each chunk buffer and of each accumulator,
+    // and a final commit on the drain barrier (each waited for at most about a second).
     if (issued >= 1) {
-      bool drained = tc_wait_own(b_done + 8u * ((issued - 1) & 1u), ((issued - 1) >> 1) & 1u);
-      if (issued >= 2)
-        drained &= tc_wait_own(b_done + 8u * ((issued - 2) & 1u), ((issued - 2) >> 1) & 1u);
+      bool drained = true;
+      for (uint32_t j = 1; j <= NB && j <= issued; j++)  // the last use of each chunk buffer
+        drained &= tc_wait_own(b_done + 8u * ((issued - j) % NB), ((issued - j) / NB) & 1u);
       const uint32_t tiles_full = issued / a.nch;  // tiles whose accumulator commit was issued
       for (uint32_t j = 1; j <= kTcAcc && j <= tiles_full; j++)  // the last use of each accumulator
         drained &= tc_wait_own(b_full + 8u * ((tiles_full - j) % kTcAcc), ((tiles_full - j) / kTcAcc) & 1u);
-      tc_commit(tc_smem_u32(bars + 4 + 2 * kTcAcc));
-      drained &= tc_wait_own(tc_smem_u32(bars + 4 + 2 * kTcAcc), 0u);
+      tc_commit(tc_smem_u32(bars + kDrain));
+      drained &= tc_wait_own(tc_smem_u32(bars + kDrain), 0u);
       if (!drained) *gave_up = 1u;
     }
   }

@@ -26,9 +26,11 @@ def run(eng, Q, k):
 
 # rows not a multiple of 128 (a partial last tile); cols covering one partial chunk (200),
 # a partial last chunk (500, 900) and four full chunks (1024); 130 queries = a full block and
-# a block of two; the three quantisers; one and 32 partitions
+# a block of two; the three quantisers; one and 32 partitions; three chunk buffers, and two
+# where the thresholds of 32 partitions leave no room for a third (1024 columns)
 @pytest.mark.parametrize("rows,cols,quant,split,ck,nq", [
     (20000, 1024, 0, 1, 1024, 130),
+    (12000, 1024, 1, 32, 512, 40),
     (20000, 1024, 1, 1, 256, 128),
     (9000, 500, 2, 32, 512, 64),
     (7777, 200, 0, 32, 512, 20),
