@@ -11,8 +11,9 @@ batched sparse-query workload it was written for.
 2. Sample stride and candidate pass: for each split's CK, every (stride, pass) of the grid is
    timed on the sample batch (wall time of aes_run, repairs included); the fastest wins.  The
    passes are the plain one (one query per matrix read), the dp4a batched one (128 queries per
-   read) and, for 4-bit matrices created with AES_FLAG_TENSOR, the tensor-core batched one
-   (FP8 tcgen05 products of 128-row tiles; same results).
+   read) with 16 (the most that fit at 1024 columns), 12 or 8 warps per CTA and, for 4-bit
+   matrices created with AES_FLAG_TENSOR, the tensor-core batched one (FP8 tcgen05 products of
+   128-row tiles; same results).
 
 Every trial re-plans the handle with aes_retune; the packed matrix stays resident.
 
@@ -65,13 +66,15 @@ def _time_runs(eng, queries, k, reps):
     return best, st["repaired"]
 
 
-PASSES = ((1, False), (128, False), (128, True))  # (batch_tile, tensor cores)
+# (batch_tile, tensor cores, warps per CTA of the dp4a batched pass; 0 = the most that fit)
+PASSES = ((1, False, 0), (128, False, 0), (128, False, 12), (128, False, 8), (128, True, 0))
 
 
 def tune(eng: E.SpMV, queries, k, ck_ladder=CK_LADDER, splits=(1,), strides=(0, 16, 64, 256),
          passes=PASSES, target=1.0, reps=3, log=None):
     """Choose CK, split, sample stride and candidate pass for `queries` (FP32 [nq, cols]) at
-    K=k.  The returned params hold batch_tile and flags (AES_FLAG_TENSOR or 0).
+    K=k.  The returned params hold batch_tile, batch_warps and flags (AES_FLAG_TENSOR or 0).
+    A pass is (batch_tile, tensor) or (batch_tile, tensor, batch_warps).
 
     Returns {"params": chosen aes_params fields, "ck_trials": [...], "time_trials": [...],
     "exact": the FP32-only Top-K rows of the sample}.  The handle is left retuned to the
@@ -80,7 +83,7 @@ def tune(eng: E.SpMV, queries, k, ck_ladder=CK_LADDER, splits=(1,), strides=(0, 
     Q = np.ascontiguousarray(np.atleast_2d(queries), np.float32)
     nq = Q.shape[0]
     base = eng.params.flags & ~E.FLAG_TENSOR
-    eng.retune(max_batch=nq, k_max=max(k, 1), flags=base)
+    eng.retune(max_batch=nq, k_max=max(k, 1), flags=base, batch_warps=0)
     eng.Q_reset(Q)
     exact, _, _ = eng.run_exact(k=k)
 
@@ -108,26 +111,29 @@ def tune(eng: E.SpMV, queries, k, ck_ladder=CK_LADDER, splits=(1,), strides=(0, 
     time_trials = []
     best = None
     for split, ck in chosen_ck.items():
-        for tile, tensor in passes:
+        for pas in passes:
+            tile, tensor, warps = (tuple(pas) + (0,))[:3]
             if tile == 128 and nq < 16:
                 continue
             flags = base | (E.FLAG_TENSOR if tensor else 0)
             for stride in strides:
                 eng.retune(ck=ck, split=split, max_batch=nq, batch_tile=tile,
-                           sample_stride=stride, flags=flags)
+                           sample_stride=stride, flags=flags, batch_warps=warps)
                 if tensor and not eng.info()["tensor_tiles"]:
                     break  # no tensor-core layout for this matrix or split
+                if warps and eng.info()["batch_warps"] != warps:
+                    break  # fewer warps fit: the trial of the most that fit covers it
                 sec, repaired = _time_runs(eng, Q, k, reps)
                 row = {"split": split, "ck": ck, "batch_tile": tile, "tensor": tensor,
-                       "sample_stride": stride, "ms_per_query": sec * 1e3 / nq,
-                       "repaired": int(repaired)}
+                       "batch_warps": warps, "sample_stride": stride,
+                       "ms_per_query": sec * 1e3 / nq, "repaired": int(repaired)}
                 time_trials.append(row)
                 if log:
                     log(row)
                 if best is None or row["ms_per_query"] < best["ms_per_query"]:
                     best = row
     params = {"ck": best["ck"], "split": best["split"], "batch_tile": best["batch_tile"],
-              "sample_stride": best["sample_stride"],
+              "sample_stride": best["sample_stride"], "batch_warps": best["batch_warps"],
               "flags": base | (E.FLAG_TENSOR if best["tensor"] else 0)}
     eng.retune(max_batch=nq, **params)
     return {"params": params, "ck_trials": ck_trials, "time_trials": time_trials,

@@ -548,7 +548,8 @@ int Engine::apply_config(const Config& c) {
       &occ, (const void*)pick_plain((int)bits, sgn, MODE_FILTER), plain_threads((int)bits), plain_smem));
   plain_grid = std::max(1, occ) * sm_count;
   batch_mode = p.batch_tile;
-  batch_warps_n = batch_warps((int)bits, cols, split);
+  batch_warps_n = batch_warps((int)bits, cols, split);  // the most that fit
+  if (p.batch_warps && (int)p.batch_warps < batch_warps_n) batch_warps_n = (int)p.batch_warps;
   if (batch_warps_n < 1) batch_mode = 1;  // query table does not fit: plain passes only
   if (batch_mode != 1) {
     batch_smem = batch_smem_bytes((int)bits, cols, split, batch_warps_n);
@@ -1109,6 +1110,7 @@ static int validate_params(const aes_params* p, uint32_t rows, uint32_t cols) {
   if (p->ck / S * S > 4096) return fail(AES_ERR_UNSUPPORTED, "ck above 4096");
   if (p->k_max == 0 || p->k_max > 1024) return fail(AES_ERR_UNSUPPORTED, "k_max must be in [1, 1024]");
   if (p->max_batch == 0 || p->max_batch > 65535) return fail(AES_ERR_INVALID, "max_batch out of range");
+  if (p->batch_warps > 32) return fail(AES_ERR_INVALID, "batch_warps above 32");
   return AES_OK;
 }
 
@@ -1287,6 +1289,7 @@ int aes_get_info(const aes_handle* h, aes_info* info) {
   info->batch_tile = e.batch_mode == 1 ? 1 : aes::dev::kBatchQ;
   info->tensor_tiles = e.use_tc ? 1u : 0u;
   info->exact_pass = e.has_f32 ? 1u : 0u;
+  info->batch_warps = e.batch_mode == 1 ? 0u : (uint32_t)e.batch_warps_n;
   return AES_OK;
 }
 

@@ -63,7 +63,8 @@ class Params(ctypes.Structure):
                 ("max_batch", ctypes.c_uint32), ("pack_parts", ctypes.c_uint32),
                 ("sample_stride", ctypes.c_uint32), ("batch_tile", ctypes.c_uint32),
                 ("device", ctypes.c_int32), ("flags", ctypes.c_uint32),
-                ("seed", ctypes.c_uint64), ("mem_limit", ctypes.c_uint64)]
+                ("seed", ctypes.c_uint64), ("mem_limit", ctypes.c_uint64),
+                ("batch_warps", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -81,7 +82,8 @@ class Info(ctypes.Structure):
                 ("ck", ctypes.c_uint32), ("ck_effective", ctypes.c_uint32),
                 ("sample_tiles", ctypes.c_uint32), ("sample_rows", ctypes.c_uint32),
                 ("max_batch", ctypes.c_uint32), ("batch_tile", ctypes.c_uint32),
-                ("tensor_tiles", ctypes.c_uint32), ("exact_pass", ctypes.c_uint32)]
+                ("tensor_tiles", ctypes.c_uint32), ("exact_pass", ctypes.c_uint32),
+                ("batch_warps", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -440,8 +442,8 @@ class SpMV:
         return SpMV(self.rows, self.cols, _view_of=self, **prm)
 
     def retune(self, **changes):
-        """Change ck, split, sample_stride, batch_tile, k_max, max_batch, flags, query_quant or
-        mem_limit without packing the matrix again; loaded queries are dropped."""
+        """Change ck, split, sample_stride, batch_tile, batch_warps, k_max, max_batch, flags,
+        query_quant or mem_limit without packing the matrix again; loaded queries are dropped."""
         prm = Params()
         ctypes.memmove(ctypes.byref(prm), ctypes.byref(self.params), ctypes.sizeof(Params))
         for k, v in changes.items():

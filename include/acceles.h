@@ -64,6 +64,9 @@ typedef struct aes_params {
   uint32_t flags;         /* AES_FLAG_* bits */
   uint64_t seed;          /* seed of the empty-row rule (check_empty_rows is unseeded) */
   uint64_t mem_limit;     /* device bytes this handle may allocate; 0 = no limit */
+  uint32_t batch_warps;   /* warps per CTA of the batched dp4a pass (0 = auto: the most whose
+                             element records fit in shared memory next to the query table, at
+                             most 16); a larger value is lowered to that */
 } aes_params;
 
 /* params.flags bits */
@@ -105,6 +108,7 @@ typedef struct aes_info {
   uint32_t tensor_tiles;  /* 1 when the batched candidate pass runs on the tensor cores */
   uint32_t exact_pass;    /* 1 when FP32 values are resident (the final Top-K is rescored in
                              FP32); 0 for a pre-quantised matrix created without them */
+  uint32_t batch_warps;   /* warps per CTA of the batched dp4a pass (0: plain passes only) */
 } aes_info;
 
 /* Defaults: bits 6, AES_QUANT_SYM_GLOBAL, AES_QQ_NUMPY, split 32, ck 512, k_max 100

@@ -17,7 +17,8 @@ class FakeEngine:
 
     def __init__(self, layout, cost, good_ck=256, nq=8, k=5):
         self.params = types.SimpleNamespace(flags=E.FLAG_GRAPHS, ck=1024, split=1, batch_tile=0,
-                                            sample_stride=0, max_batch=nq, k_max=k)
+                                            sample_stride=0, max_batch=nq, k_max=k,
+                                            batch_warps=0)
         self.layout, self.cost, self.good_ck, self.k = layout, cost, good_ck, k
         self.exact = np.arange(nq * k, dtype=np.uint32).reshape(nq, k)
         self.calls = []
@@ -29,7 +30,8 @@ class FakeEngine:
 
     def info(self):
         t = bool(self.params.flags & E.FLAG_TENSOR) and self.layout and self.params.batch_tile != 1
-        return {"tensor_tiles": 1 if t else 0, "split": self.params.split}
+        w = (self.params.batch_warps or 16) if self.params.batch_tile != 1 else 0
+        return {"tensor_tiles": 1 if t else 0, "split": self.params.split, "batch_warps": w}
 
     def Q_reset(self, q):
         self.nq = len(q)
@@ -61,8 +63,9 @@ def test_tune_times_every_pass_and_keeps_the_fastest(layout, fastest):
     # the ladder stopped at the first CK with the exact Top-K
     assert [t["ck"] for t in res["ck_trials"]] == [128, 256]
     assert res["params"]["ck"] == 256
-    passes = {(t["batch_tile"], t["tensor"]) for t in res["time_trials"]}
-    want = {(1, False), (128, False)} | ({(128, True)} if layout else set())
+    passes = {(t["batch_tile"], t["tensor"], t["batch_warps"]) for t in res["time_trials"]}
+    want = {(1, False, 0), (128, False, 0), (128, False, 12), (128, False, 8)}
+    want |= {(128, True, 0)} if layout else set()
     assert passes == want
     p = res["params"]
     assert (p["flags"] & E.FLAG_TENSOR != 0) == (fastest == "tensor")

@@ -248,6 +248,32 @@ def test_batched_short_rows(bits, lo, hi):
         assert np.array_equal(gi, exp), i
 
 
+@pytest.mark.parametrize("warps", [1, 3, 8, 12])
+def test_batched_warps_per_cta(warps):
+    """Fewer warps per CTA than fit (aes_params.batch_warps) give the same results: the tiles a
+    CTA takes, and so the ranges its warps walk, change with the warp count."""
+    rows, cols, k, nq = 25000, 1024, 100, 130
+    m, eng = make(rows, cols, E.GEN_UNIFORM_DEG, 10, 30, 5 + warps, 8, 0, 1, 512, k, nq=nq,
+                  batch_tile=128)
+    Q = queries(cols, nq, 23, signed=True)
+    eng.Q_reset(Q)
+    eng(k=k)
+    ref = tuple(x.copy() for x in eng.read_topk())
+    assert eng.info()["batch_warps"] == 16
+    eng.retune(batch_warps=warps)
+    assert eng.info()["batch_warps"] == warps
+    eng.Q_reset(Q)
+    eng(k=k)
+    idx, sc = eng.read_topk()
+    assert np.array_equal(idx, ref[0]) and np.array_equal(sc, ref[1])
+    for i in range(0, nq, 16):
+        oi, os_, _ = m.two_stage(Q[i], 1, 512, k)
+        assert np.array_equal(idx[i, :len(oi)], oi) and np.array_equal(sc[i, :len(oi)], os_), i
+    with pytest.raises(E.AesError) as ei:  # above the 32 warps a CTA can hold
+        eng.retune(batch_warps=40)
+    assert ei.value.code == E.AES_ERR_INVALID
+
+
 def test_batched_equals_plain_and_long_rows():
     rows, cols = 6000, 700
     ptr, col, val = E.gen_matrix(E.GEN_GAMMA_DEG, rows, cols, 120, 700, seed=77)

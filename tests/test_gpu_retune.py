@@ -87,9 +87,15 @@ def test_autotune_reaches_target_and_leaves_handle_tuned():
                   strides=(0, 16), reps=1)
     prm = res["params"]
     assert eng.info()["split"] == prm["split"]
-    # all three candidate passes were timed; the handle runs the chosen one
-    assert {(t["batch_tile"], t["tensor"]) for t in res["time_trials"]} == set(AT.PASSES)
-    assert eng.info()["tensor_tiles"] == (1 if prm["flags"] & E.FLAG_TENSOR else 0)
+    # every candidate pass of the grid was timed (plain, dp4a at 16, 12 and 8 warps per CTA,
+    # tensor cores); the handle runs the chosen one
+    assert {(t["batch_tile"], t["tensor"], t["batch_warps"]) for t in res["time_trials"]} == set(AT.PASSES)
+    inf = eng.info()
+    assert inf["tensor_tiles"] == (1 if prm["flags"] & E.FLAG_TENSOR else 0)
+    if prm["batch_tile"] == 128 and not inf["tensor_tiles"]:
+        assert inf["batch_warps"] > 0
+        if prm["batch_warps"]:
+            assert inf["batch_warps"] == prm["batch_warps"]
     # the chosen configuration reproduces the FP32-only Top-K on every sample query
     eng.Q_reset(Q)
     eng(k=k)
@@ -141,7 +147,7 @@ def test_autotune_ck_equals_oracle_brute_force():
     Q = _queries(cols, nq, 29)
     ladder, splits = (64, 128, 256, 512, 1024), (1, 32)
     res = AT.tune(eng, Q, k, ck_ladder=ladder, splits=splits, strides=(0, 16), reps=1,
-                  passes=((1, False), (128, False)))
+                  passes=((1, False), (128, False), (128, False, 8)))
     xi, _ = orc.topk_f32_many(m.ptr, m.col, m.val, rows, cols, Q, k)
     for split in splits:
         want = None
@@ -158,3 +164,4 @@ def test_autotune_ck_equals_oracle_brute_force():
     assert res["params"]["ck"] == best["ck"] and res["params"]["split"] == best["split"]
     assert res["params"]["batch_tile"] == best["batch_tile"]
     assert res["params"]["sample_stride"] == best["sample_stride"]
+    assert res["params"]["batch_warps"] == best["batch_warps"]
