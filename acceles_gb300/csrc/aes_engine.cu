@@ -213,6 +213,12 @@ struct Engine {
   size_t tc_smem = 0;
   int tc_grid = 0;
   uint32_t tc_nb = 2;  // chunk buffers of the tensor-core pass (tc_bufs)
+  // the CTA-pair form (two 128-query blocks per launch), where a pair's shared memory fits and
+  // clusters of two CTAs of that size can be scheduled
+  bool tc_pair = false;
+  size_t tc_smem2 = 0;
+  int tc_grid2 = 0;
+  uint32_t tc_nb2 = 2;
   bool last_batched = false;
   std::vector<uint32_t> h_tile_rowbase;  // host copy: sample geometry is derived from it
   size_t bytes = 0, mat_bytes = 0, cfg_bytes = 0;
@@ -299,7 +305,7 @@ struct Engine {
              uint32_t* repaired);
   int run_plain(int mode, uint32_t q, cudaStream_t s, uint32_t nq_y = 1);
   int run_batch(int mode, uint32_t nq, cudaStream_t s, uint32_t blk0 = 0, uint32_t nblk = 0);
-  int run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s);
+  int run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s, bool pair);
   int prof_open(cudaStream_t s);
   int prof_close(cudaStream_t s);
   int collect_profile();
@@ -307,7 +313,7 @@ struct Engine {
   // every partition in shared memory, batched passes allowed
   bool tc_usable(const aes_params& p, uint32_t S) const {
     return tc_ready && (p.flags & AES_FLAG_TENSOR) && S <= kTcMaxSplit && p.batch_tile != 1 &&
-           tc_smem_bytes(cols, S, 2) <= (size_t)smem_optin;
+           tc_smem_bytes(cols, S, 2, false) <= (size_t)smem_optin;
   }
 };
 
@@ -334,10 +340,11 @@ int Engine::prof_close(cudaStream_t s) {
   return AES_OK;
 }
 
-// Batched candidate pass of one block of <= 128 queries on the tensor cores (aes_tc.cuh); its
-// query blocks are those of the dp4a pass, whose sample pass it shares
+// Batched candidate pass on the tensor cores (aes_tc.cuh) of one block of <= 128 queries, or
+// (pair) of blocks blk and blk + 1 (<= 256 queries) by CTA pairs; its query blocks are those of
+// the dp4a pass, whose sample pass it shares
 static_assert(kTcQ == kBatchQ, "tensor-core and dp4a passes use the same query blocks");
-int Engine::run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
+int Engine::run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s, bool pair) {
   TcArgs a{};
   a.ent = d_tc_ent;
   a.ptr = d_tc_ptr;
@@ -360,10 +367,26 @@ int Engine::run_tc(uint32_t blk, uint32_t nq_blk, cudaStream_t s) {
   const bool prof = (prm.flags & AES_FLAG_PROFILE) != 0;
   int rc = prof ? prof_open(s) : AES_OK;
   if (rc) return rc;
-  if (tc_nb == 3)
-    k_cand_tc<3><<<tc_grid, kTcThreads, tc_smem, s>>>(a);
-  else
-    k_cand_tc<2><<<tc_grid, kTcThreads, tc_smem, s>>>(a);
+  if (pair) {  // clusters of two CTAs: a pair per two SMs
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)tc_grid2);
+    cfg.blockDim = dim3(kTcThreads);
+    cfg.dynamicSmemBytes = tc_smem2;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    AES_CK(tc_nb2 == 3 ? cudaLaunchKernelEx(&cfg, k_cand_tc<3, true>, a)
+                       : cudaLaunchKernelEx(&cfg, k_cand_tc<2, true>, a));
+  } else if (tc_nb == 3) {
+    k_cand_tc<3, false><<<tc_grid, kTcThreads, tc_smem, s>>>(a);
+  } else {
+    k_cand_tc<2, false><<<tc_grid, kTcThreads, tc_smem, s>>>(a);
+  }
   AES_CK(cudaGetLastError());
   if (prof && (rc = prof_close(s))) return rc;
   n_launch++;
@@ -559,9 +582,34 @@ int Engine::apply_config(const Config& c) {
     batch_grid = std::max(1, occb) * sm_count;
   }
   if (use_tc) {  // one CTA per SM (its shared memory), persistent over the 128-row tiles
-    tc_nb = tc_bufs(cols, split, (size_t)smem_optin);
-    tc_smem = tc_smem_bytes(cols, split, tc_nb);
+    tc_nb = tc_bufs(cols, split, (size_t)smem_optin, false);
+    tc_smem = tc_smem_bytes(cols, split, tc_nb, false);
     tc_grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)sm_count, tc_rtiles));
+    tc_pair = false;
+    if (tc_smem_bytes(cols, split, 2, true) <= (size_t)smem_optin && sm_count >= 2) {
+      tc_nb2 = tc_bufs(cols, split, (size_t)smem_optin, true);
+      tc_smem2 = tc_smem_bytes(cols, split, tc_nb2, true);
+      const uint32_t pairs = std::max<uint32_t>(
+          1, std::min<uint32_t>((uint32_t)sm_count / 2, (tc_rtiles + 1) / 2));
+      tc_grid2 = 2 * (int)pairs;
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)tc_grid2);
+      cfg.blockDim = dim3(kTcThreads);
+      cfg.dynamicSmemBytes = tc_smem2;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      const cudaError_t e = tc_nb2 == 3
+          ? cudaOccupancyMaxActiveClusters(&nclusters, k_cand_tc<3, true>, &cfg)
+          : cudaOccupancyMaxActiveClusters(&nclusters, k_cand_tc<2, true>, &cfg);
+      if (e == cudaSuccess && nclusters > 0) tc_pair = true;
+      else (void)cudaGetLastError();  // the single-CTA form serves every block
+    }
   } else {
     d_qtab_tc = nullptr;
   }
@@ -688,8 +736,10 @@ int Engine::build(const HostCSR& m, const aes_params& p) {
     AES_CK(raise_smem((const void*)pick_batch((int)bits, sgn, mode)));
   AES_CK(raise_smem((const void*)k_final));
   if (tc_ready) {
-    AES_CK(raise_smem((const void*)k_cand_tc<2>));
-    AES_CK(raise_smem((const void*)k_cand_tc<3>));
+    AES_CK(raise_smem((const void*)k_cand_tc<2, false>));
+    AES_CK(raise_smem((const void*)k_cand_tc<3, false>));
+    AES_CK(raise_smem((const void*)k_cand_tc<2, true>));
+    AES_CK(raise_smem((const void*)k_cand_tc<3, true>));
   }
   // the matrix arrays go to the store a view shares; the slow path's key array stays the handle's
   mat_store = std::make_shared<SharedAllocs>();
@@ -914,10 +964,13 @@ int Engine::enqueue(const float* d_q, uint32_t nq, uint32_t k, uint32_t* d_idx, 
   AES_CK(cudaGetLastError());
   if (batched) {
     if (use_tc) {
-      for (uint32_t b = 0; b < nblk; b++) {
-        const uint32_t nb = std::min<uint32_t>(kBatchQ, nq - b * kBatchQ);
-        int rc = run_tc(b, nb, s);
+      // two blocks per launch by CTA pairs where there are two; a last odd block alone
+      for (uint32_t b = 0; b < nblk;) {
+        const bool pair = tc_pair && b + 1 < nblk;
+        const uint32_t nb = std::min<uint32_t>((pair ? 2u : 1u) * kBatchQ, nq - b * kBatchQ);
+        int rc = run_tc(b, nb, s, pair);
         if (rc) return rc;
+        b += pair ? 2u : 1u;
       }
     } else {
       int rc = run_batch(MODE_FILTER, nq, s);

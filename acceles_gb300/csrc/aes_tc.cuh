@@ -41,23 +41,33 @@ constexpr int kTcEpiWarp = 8;
 constexpr int kTcEpilogue = 256;
 constexpr int kTcMmaWarp = 16;
 constexpr int kTcThreads = 17 * 32;
-constexpr uint32_t kTcAcc = 4;  // FP32 accumulators in tensor memory
-constexpr uint32_t kTcTmemCols = kTcAcc * kTcQ;
-// mbarriers of a kernel with NB chunk buffers: staged[NB] (producers -> MMA), done[NB] (MMA ->
-// producers), full[kTcAcc] (MMA -> epilogue), empty[kTcAcc] (epilogue -> MMA), drain (the MMA
-// thread's own MMAs complete); then the tensor-memory address and the give-up flag
-__host__ __device__ constexpr uint32_t tc_nbars(uint32_t nb) { return 2 * nb + 2 * kTcAcc + 1; }
+constexpr uint32_t kTcTmemCols = 512;  // all of tensor memory, in FP32 accumulators
+// Queries per launch and accumulators.  One CTA: 128 queries (N = 128, M = 128), four
+// accumulators of 128 columns.  A CTA pair (cta_group::2): 256 queries (N = 256, each CTA
+// holding 128 of them in its operand) and M = 256 (each CTA's 128-row tile), two accumulators
+// of 256 columns in each CTA's tensor memory.
+template <bool PAIR>
+struct TcShape {
+  static constexpr uint32_t Q = PAIR ? 2 * kTcQ : kTcQ;
+  static constexpr uint32_t ACC = kTcTmemCols / Q;
+};
+// mbarriers of a kernel with nb chunk buffers and acc accumulators: staged[nb] (producers ->
+// MMA), done[nb] (MMA -> producers), full[acc] (MMA -> epilogue), empty[acc] (epilogue -> MMA),
+// drain (the MMA thread's own MMAs complete); then the tensor-memory address and the give-up
+// flag
+__host__ __device__ constexpr uint32_t tc_nbars(uint32_t nb, uint32_t acc) { return 2 * nb + 2 * acc + 1; }
 
-// shared memory of the pass with nb chunk buffers (2 or 3)
-__host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split, uint32_t nb) {
+// shared memory of one CTA of the pass with nb chunk buffers (2 or 3)
+__host__ inline size_t tc_smem_bytes(uint32_t cols, uint32_t split, uint32_t nb, bool pair) {
   const uint32_t S = split <= 1 ? 1 : split;
-  return tc_qtab_bytes(cols) + nb * (size_t)kTcChunkBytes + (size_t)S * kTcQ * 4 +
-         ((tc_nbars(nb) * 8 + 8 + 15) & ~15u);
+  const uint32_t q = pair ? 2 * kTcQ : kTcQ;
+  return tc_qtab_bytes(cols) + nb * (size_t)kTcChunkBytes + (size_t)S * q * 4 +
+         ((tc_nbars(nb, kTcTmemCols / q) * 8 + 8 + 15) & ~15u);
 }
 // chunk buffers for a configuration: three where they fit next to the query operand and the
 // thresholds (the producers then run two chunks ahead of the MMAs), else two
-__host__ inline uint32_t tc_bufs(uint32_t cols, uint32_t split, size_t smem_limit) {
-  return tc_smem_bytes(cols, split, 3) <= smem_limit ? 3u : 2u;
+__host__ inline uint32_t tc_bufs(uint32_t cols, uint32_t split, size_t smem_limit, bool pair) {
+  return tc_smem_bytes(cols, split, 3, pair) <= smem_limit ? 3u : 2u;
 }
 
 // e4m3 query operand of queries q0 .. q0 + nq - 1 (zero past nq and past cols)
@@ -101,14 +111,30 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
 // Waits for the phase of the given parity to complete, for about a second at most, whether or
 // not another role has given up: the MMA thread's wait for its own MMAs in flight before the CTA
 // frees its tensor memory and leaves.
-__device__ __forceinline__ bool tc_wait_own(uint32_t bar, uint32_t parity) {
-  const long long t0 = clock64();
-  uint32_t done = 0;
-  while (!done) {
+// CL: acquire at cluster scope (a barrier that the peer CTA of a pair arrives on, or whose
+// phase orders work of the peer).
+template <bool CL>
+__device__ __forceinline__ uint32_t tc_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  if constexpr (CL) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+  } else {
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+  }
+  return done;
+}
+template <bool CL = false>
+__device__ __forceinline__ bool tc_wait_own(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  uint32_t done = 0;
+  while (!done) {
+    done = tc_try<CL>(bar, parity);
     if (!done && clock64() - t0 > (1ll << 31)) return false;
   }
   return true;
@@ -116,14 +142,12 @@ __device__ __forceinline__ bool tc_wait_own(uint32_t bar, uint32_t parity) {
 // Waits for the phase of the given parity to complete.  Gives up after about a second, or as
 // soon as another thread of the CTA has given up (*gave_up set), so that every role leaves its
 // loop instead of waiting on a partner that has left.
+template <bool CL = false>
 __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile uint32_t* gave_up) {
   const long long t0 = clock64();
   uint32_t done = 0;
   while (!done) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    done = tc_try<CL>(bar, parity);
     if (done) break;
     if (*gave_up) return false;
     if (clock64() - t0 > (1ll << 31)) {
@@ -142,16 +166,69 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
+// Arrives on a barrier of the pair's even CTA (the one whose thread issues the MMAs): through
+// its shared::cluster address, with release at cluster scope.  One CTA: a local arrive.
+template <bool PAIR>
+__device__ __forceinline__ void tc_arrive_leader(uint32_t bar) {
+  if constexpr (PAIR) {
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(ra) : "r"(bar));
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" :: "r"(ra) : "memory");
+  } else {
+    tc_arrive(bar);
+  }
+}
+template <bool PAIR>
 __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t da, uint64_t db, uint32_t idesc,
                                        uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
-      :: "r"(d), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+  if constexpr (PAIR) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+        :: "r"(d), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+        :: "r"(d), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+  }
 }
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-               :: "r"(bar) : "memory");
+// Arrives on `bar` once the MMAs issued so far complete.  PAIR: on the barrier at the same
+// offset in each CTA of ctamask (bit r: the pair's CTA of rank r).
+template <bool PAIR>
+__device__ __forceinline__ void tc_commit(uint32_t bar, uint16_t ctamask = 3) {
+  if constexpr (PAIR) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+        :: "r"(bar), "h"(ctamask) : "memory");
+  } else {
+    (void)ctamask;
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(bar) : "memory");
+  }
+}
+// Tensor memory of the CTA (PAIR: of both CTAs, the same columns, by one warp of each)
+template <bool PAIR>
+__device__ __forceinline__ void tc_alloc(uint32_t slot) {
+  if constexpr (PAIR) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(slot), "n"(kTcTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  } else {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(slot), "n"(kTcTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+}
+template <bool PAIR>
+__device__ __forceinline__ void tc_dealloc(uint32_t tmem) {
+  if constexpr (PAIR)
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" :: "r"(tmem), "n"(kTcTmemCols));
+  else
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "n"(kTcTmemCols));
+}
+__device__ __forceinline__ void tc_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 // 32 consecutive accumulator columns of this warp's 32 lanes (one row per thread)
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
@@ -167,7 +244,7 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, 64 queries) and
+// Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, half the queries) and
 // appends every (row, query) key at or above the query's threshold.  thf holds the thresholds as
 // FP32 bounds: the score (an exact integer in FP32) or rowscale * score is compared directly.
 // A block of 32 queries is compared without branches into a bit mask of hits.  The hits of a
@@ -180,19 +257,21 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 __device__ __forceinline__ uint32_t tc_epi_row(uint32_t T) {
   return T * kTcRows + ((threadIdx.x >> 5) & 3u) * 32u + (threadIdx.x & 31u);
 }
+template <bool PAIR>
 __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_t tmem,
                                             uint32_t dbuf, const float* thf_all, uint32_t S,
                                             float rs) {
+  constexpr uint32_t Q = TcShape<PAIR>::Q, HALF = Q / 2;
   const uint32_t warp = threadIdx.x >> 5;
   const uint32_t g = warp & 3u, h = (warp - kTcEpiWarp) >> 2;
   const uint32_t row = tc_epi_row(T);
   const bool valid = row < a.n_rows;
   const uint32_t p = valid ? part_of(row, S, a.slice) : 0u;
-  const float* thf = thf_all + p * kTcQ;
+  const float* thf = thf_all + p * Q;
 #pragma unroll 1
-  for (uint32_t col0 = h * 64u; col0 < h * 64u + 64u; col0 += 32u) {
+  for (uint32_t col0 = h * HALF; col0 < h * HALF + HALF; col0 += 32u) {
     uint32_t v[32];
-    tc_ld32(tmem + dbuf * kTcQ + col0 + ((g * 32u) << 16), v);
+    tc_ld32(tmem + dbuf * Q + col0 + ((g * 32u) << 16), v);
     uint32_t hit = 0;
 #pragma unroll
     for (int j4 = 0; j4 < 8; j4++) {  // the same 32 thresholds for every lane: 16-byte broadcasts
@@ -266,34 +345,49 @@ __device__ __forceinline__ bool tc_producers_any(bool fail) {
   return r != 0;
 }
 
-// One CTA per SM, persistent over row tiles T = blockIdx.x, + gridDim.x, ...  Chunk i of the CTA
-// is chunk i % nch of its tile i / nch; chunk buffer i % NB; accumulator (tile t) t % kTcAcc.
-template <uint32_t NB>
+
+// One CTA per SM (PAIR: one CTA pair, a cluster of two, per two SMs), persistent over units of
+// work U = unit, unit + units, ...: a 128-row tile (one CTA), or two consecutive tiles, 2U for
+// the even CTA and 2U + 1 for the odd one (PAIR).  Chunk i of the CTA is chunk i % nch of its
+// unit i / nch; chunk buffer i % NB; accumulator (unit t) t % ACC.
+// PAIR: the even CTA's MMA thread issues cta_group::2 MMAs with M = 256 (the two CTAs' row tiles
+// from their own chunk buffers) and N = 256 (the two CTAs' 128-query operands), and commits them
+// to the barriers of both CTAs; both CTAs' producers and epilogues hand their buffers and
+// accumulators back to the even CTA's barriers.  The two CTAs keep identical shared-memory
+// layouts, since an operand descriptor addresses the same offset in both.
+template <uint32_t NB, bool PAIR>
 __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   static_assert(NB == 2 || NB == 3, "two or three chunk buffers");
-  constexpr uint32_t kDone = NB, kFull = 2 * NB, kEmpty = 2 * NB + kTcAcc;
-  constexpr uint32_t kDrain = kEmpty + kTcAcc, kBars = tc_nbars(NB);
+  constexpr uint32_t Q = TcShape<PAIR>::Q, ACC = TcShape<PAIR>::ACC;
+  constexpr uint32_t kDone = NB, kFull = 2 * NB, kEmpty = 2 * NB + ACC;
+  constexpr uint32_t kDrain = kEmpty + ACC, kBars = tc_nbars(NB, ACC);
   constexpr uint32_t R = NB + 2;  // producer ring: the chunks of every buffer and two ahead
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t qbytes = (a.kpad / 16u) * 2048u;
-  unsigned char* sq = smem;                     // query operand
+  unsigned char* sq = smem;                     // query operand (PAIR: this CTA's 128 queries)
   unsigned char* sa = smem + qbytes;            // NB chunk buffers of the row tile
   float* thf = reinterpret_cast<float*>(sa + NB * kTcChunkBytes);
   const uint32_t S = a.split <= 1 ? 1u : a.split;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * kTcQ);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(thf + S * Q);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kBars);
   volatile uint32_t* gave_up = tslot + 1;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  uint32_t rank = 0;  // the CTA's rank in its pair
+  if constexpr (PAIR) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+  const uint32_t unit = PAIR ? (blockIdx.x >> 1) : blockIdx.x;
+  const uint32_t units = PAIR ? (gridDim.x >> 1) : gridDim.x;
+  const uint32_t n_units = PAIR ? (a.n_rtiles + 1u) / 2u : a.n_rtiles;
+  auto tile_of = [&](uint32_t u) { return PAIR ? 2u * u + rank : u; };  // this CTA's row tile
   {
-    const uint4* src = reinterpret_cast<const uint4*>(a.qt);
+    const uint4* src = reinterpret_cast<const uint4*>(a.qt + (PAIR ? rank * qbytes : 0u));
     uint4* dst = reinterpret_cast<uint4*>(sq);
     for (uint32_t i = tid; i < qbytes / 16u; i += blockDim.x) dst[i] = src[i];
     uint4* z = reinterpret_cast<uint4*>(sa);
     for (uint32_t i = tid; i < NB * kTcChunkBytes / 16u; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
     // thresholds as FP32 bounds on the score (int keys) or on rowscale * score:
     // key >= th  <=>  x >= bound for every x the pass produces
-    for (uint32_t i = tid; i < S * kTcQ; i += blockDim.x) {
-      const uint32_t p = i / kTcQ, q = i % kTcQ;
+    for (uint32_t i = tid; i < S * Q; i += blockDim.x) {
+      const uint32_t p = i / Q, q = i % Q;
       const uint32_t th = q < a.nq ? a.thr[(size_t)(a.q0 + q) * S + p] : 0xFFFFFFFFu;
       float fb;
       if (a.rowscale) {  // x >= +0, key(x) = bits(x) | 2^31; NaN bits: never
@@ -308,27 +402,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   }
   if (tid == 0) {
     for (uint32_t b = 0; b < kBars; b++) {
-      const uint32_t cnt = (b < kDone) ? (uint32_t)kTcProducers
-                                       : ((b >= kEmpty && b < kDrain) ? (uint32_t)kTcEpilogue : 1u);
+      // The roles arrive on their own CTA's staged and empty barriers.  PAIR: a thread of the
+      // odd CTA forwards each completed phase of those to the even CTA's, which therefore take
+      // one arrival more (a release at cluster scope costs about a thousand cycles: forwarded,
+      // it stays off the producers' and the epilogue's paths)
+      const uint32_t fwd = (PAIR && rank == 0) ? 1u : 0u;
+      const uint32_t cnt = (b < kDone) ? (uint32_t)kTcProducers + fwd
+                                       : ((b >= kEmpty && b < kDrain) ? (uint32_t)kTcEpilogue + fwd : 1u);
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tc_smem_u32(bars + b)), "r"(cnt));
     }
     *gave_up = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == kTcMmaWarp) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 :: "r"(tc_smem_u32(tslot)), "n"(kTcTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
+  if (warp == kTcMmaWarp) tc_alloc<PAIR>(tc_smem_u32(tslot));
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) tc_cluster_sync();  // both CTAs' barriers exist before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tslot;
   const uint32_t b_staged = tc_smem_u32(bars), b_done = tc_smem_u32(bars + kDone);
   const uint32_t b_full = tc_smem_u32(bars + kFull), b_empty = tc_smem_u32(bars + kEmpty);
-  const uint32_t ntl = a.n_rtiles > blockIdx.x ? (a.n_rtiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
-  const uint32_t total = ntl * a.nch;  // chunks of this CTA
+  const uint32_t ntl = n_units > unit ? (n_units - unit + units - 1) / units : 0u;
+  const uint32_t total = ntl * a.nch;  // chunks of this CTA (PAIR: the same in both CTAs)
   bool ok = true;
 
   if (warp < kTcProducers / 32) {
@@ -338,18 +434,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     // from E[(i + 2) % R], loads chunk i + 2 into that set and stages chunk i (loaded two steps
     // earlier); a chunk's row offsets are read R steps before its entries.  So no register a
     // store or a copy reads waits on a load in flight.
-    // chunk id of chunk i: tile blockIdx.x + (i / nch) gridDim.x, chunk i % nch; kept
-    // incrementally for the look-ahead chunk (no division per step)
-    uint32_t la_i = 0, la_t = blockIdx.x, la_c = 0;
+    // chunk id of chunk i: tile tile_of(unit + (i / nch) units), chunk i % nch; kept
+    // incrementally for the look-ahead chunk (no division per step).  PAIR: the odd CTA's tile
+    // of the last unit may lie past the matrix; its chunks are empty.
+    uint32_t la_i = 0, la_t = tile_of(unit), la_c = 0;
     auto ptr_next = [&](uint32_t& b, uint32_t& e) {  // offsets of chunk la_i, then advance it
-      const bool in = la_i < total;
+      const bool in = la_i < total && la_t < a.n_rtiles;
       const uint32_t j = la_t * a.nch + la_c;
       b = in ? __ldg(a.ptr + j) : 0u;
       e = in ? __ldg(a.ptr + j + 1) : 0u;
       la_i++;
       if (++la_c == a.nch) {
         la_c = 0;
-        la_t += gridDim.x;
+        la_t += (PAIR ? 2u : 1u) * units;
       }
     };
     TcEnt E[R];
@@ -367,7 +464,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     auto step = [&](uint32_t i, TcEnt& cur, TcEnt& old, uint32_t& pb, uint32_t& pe) -> bool {
       unsigned char* ab = sa + buf * kTcChunkBytes;
       if (i >= NB) {  // the MMAs of chunk i - NB have read this buffer: clear its entries
-        ok &= tc_wait(b_done + 8u * buf, ((i - NB) / NB) & 1u, gave_up);
+        ok &= tc_wait<PAIR>(b_done + 8u * buf, ((i - NB) / NB) & 1u, gave_up);
         if (ok) old.stage(ab, a.ent, tid, true);
       }
       // every clear lands before any write of this chunk (they may share a byte); the
@@ -393,35 +490,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
   } else if (warp < kTcEpiWarp + kTcEpilogue / 32) {
     // ---- epilogue -----------------------------------------------------------------------------
     for (uint32_t tl = 0; tl < ntl; tl++) {
-      const uint32_t d = tl % kTcAcc;
-      const uint32_t T = blockIdx.x + tl * gridDim.x, row = tc_epi_row(T);
+      const uint32_t d = tl % ACC;
+      const uint32_t T = tile_of(unit + tl * units), row = tc_epi_row(T);
       const float rs = (a.rowscale && row < a.n_rows) ? __ldg(a.rowscale + row) : 0.0f;
-      ok &= tc_wait(b_full + 8u * d, (tl / kTcAcc) & 1u, gave_up);
+      ok &= tc_wait<PAIR>(b_full + 8u * d, (tl / ACC) & 1u, gave_up);
       ok = __all_sync(0xFFFFFFFFu, ok);  // tcgen05.ld needs the whole warp
       if (!ok) break;
       tc_fence_after();
-      tc_epilogue(a, T, tmem, d, thf, S, rs);
+      tc_epilogue<PAIR>(a, T, tmem, d, thf, S, rs);
       tc_fence_before();
       tc_arrive(b_empty + 8u * d);
     }
-  } else if ((tid & 31u) == 0) {
-    // ---- MMA issue (one thread) ---------------------------------------------------------------
-    // instruction descriptor: FP32 accumulator, e4m3 x e4m3, both K-major, N = 128, M = 128
-    const uint32_t idesc = (1u << 4) | ((kTcQ >> 3) << 17) | ((kTcRows >> 4) << 24);
+  } else if ((tid & 31u) == 0 && rank == 0) {
+    // ---- MMA issue (one thread; PAIR: of the even CTA) ----------------------------------------
+    // instruction descriptor: FP32 accumulator, e4m3 x e4m3, both K-major, N = Q, M = 128 (256
+    // over a pair)
+    const uint32_t idesc = (1u << 4) | ((Q >> 3) << 17) | (((PAIR ? 2u : 1u) * kTcRows >> 4) << 24);
     const uint32_t sq_addr = tc_smem_u32(sq), sa_addr = tc_smem_u32(sa);
     uint32_t tl = 0, c = 0, issued = 0;
     for (uint32_t i = 0; i < total && !a.mma_idle; i++) {
-      const uint32_t buf = i % NB, d = tl % kTcAcc;
-      if (c == 0 && tl >= kTcAcc) ok &= tc_wait(b_empty + 8u * d, ((tl - kTcAcc) / kTcAcc) & 1u, gave_up);
-      if (ok) ok &= tc_wait(b_staged + 8u * buf, (i / NB) & 1u, gave_up);
+      const uint32_t buf = i % NB, d = tl % ACC;
+      if (c == 0 && tl >= ACC) ok &= tc_wait<PAIR>(b_empty + 8u * d, ((tl - ACC) / ACC) & 1u, gave_up);
+      if (ok) ok &= tc_wait<PAIR>(b_staged + 8u * buf, (i / NB) & 1u, gave_up);
       if (!ok) break;
       tc_fence_after();
       const uint32_t nk = min(kTcChunkK, a.kpad - c * kTcChunkK) / 32u;
       for (uint32_t kk = 0; kk < nk; kk++)
-        tc_mma(tmem + d * kTcQ, tc_desc(sa_addr + buf * kTcChunkBytes + kk * 4096u),
-               tc_desc(sq_addr + (c * 16u + 2u * kk) * 2048u), idesc, (c | kk) != 0);
-      tc_commit(b_done + 8u * buf);
-      if (c == a.nch - 1) tc_commit(b_full + 8u * d);
+        tc_mma<PAIR>(tmem + d * Q, tc_desc(sa_addr + buf * kTcChunkBytes + kk * 4096u),
+                     tc_desc(sq_addr + (c * 16u + 2u * kk) * 2048u), idesc, (c | kk) != 0);
+      tc_commit<PAIR>(b_done + 8u * buf);
+      if (c == a.nch - 1) tc_commit<PAIR>(b_full + 8u * d);
       issued = i + 1;
       if (++c == a.nch) {
         c = 0;
@@ -435,21 +533,48 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     if (issued >= 1) {
       bool drained = true;
       for (uint32_t j = 1; j <= NB && j <= issued; j++)  // the last use of each chunk buffer
-        drained &= tc_wait_own(b_done + 8u * ((issued - j) % NB), ((issued - j) / NB) & 1u);
-      const uint32_t tiles_full = issued / a.nch;  // tiles whose accumulator commit was issued
-      for (uint32_t j = 1; j <= kTcAcc && j <= tiles_full; j++)  // the last use of each accumulator
-        drained &= tc_wait_own(b_full + 8u * ((tiles_full - j) % kTcAcc), ((tiles_full - j) / kTcAcc) & 1u);
-      tc_commit(tc_smem_u32(bars + kDrain));
-      drained &= tc_wait_own(tc_smem_u32(bars + kDrain), 0u);
+        drained &= tc_wait_own<PAIR>(b_done + 8u * ((issued - j) % NB), ((issued - j) / NB) & 1u);
+      const uint32_t tiles_full = issued / a.nch;  // units whose accumulator commit was issued
+      for (uint32_t j = 1; j <= ACC && j <= tiles_full; j++)  // the last use of each accumulator
+        drained &= tc_wait_own<PAIR>(b_full + 8u * ((tiles_full - j) % ACC), ((tiles_full - j) / ACC) & 1u);
+      tc_commit<PAIR>(tc_smem_u32(bars + kDrain), 1);
+      drained &= tc_wait_own<PAIR>(tc_smem_u32(bars + kDrain), 0u);
       if (!drained) *gave_up = 1u;
     }
+  } else if (PAIR && rank == 1 && (tid & 31u) == 1) {
+    // ---- the odd CTA: forwards each completed phase of its empty barriers (its epilogue has
+    // read the accumulator) to the even CTA's
+    for (uint32_t tl = 0; tl < ntl; tl++) {
+      const uint32_t d = tl % ACC;
+      if (!tc_wait(b_empty + 8u * d, (tl / ACC) & 1u, gave_up)) break;
+      tc_arrive_leader<PAIR>(b_empty + 8u * d);
+    }
+  } else if (PAIR && rank == 1 && (tid & 31u) == 0) {
+    // ---- the odd CTA: forwards each completed phase of its staged barriers (its producers have
+    // staged the chunk) to the even CTA's
+    for (uint32_t i = 0; i < total; i++) {
+      const uint32_t buf = i % NB;
+      if (!tc_wait(b_staged + 8u * buf, (i / NB) & 1u, gave_up)) break;
+      tc_arrive_leader<PAIR>(b_staged + 8u * buf);
+    }
+    // before the CTA leaves, the even CTA's commits to its barriers have landed (the last use of
+    // each chunk buffer and accumulator; skipped once it gave up)
+    bool drained = true;
+    for (uint32_t j = 1; j <= NB && j <= total && drained && !*gave_up; j++)
+      drained = tc_wait_own<PAIR>(b_done + 8u * ((total - j) % NB), ((total - j) / NB) & 1u);
+    for (uint32_t j = 1; j <= ACC && j <= ntl && drained && !*gave_up; j++)
+      drained = tc_wait_own<PAIR>(b_full + 8u * ((ntl - j) % ACC), ((ntl - j) / ACC) & 1u);
+    if (!drained) *gave_up = 1u;
   }
   tc_fence_before();
   __syncthreads();
+  // PAIR: neither CTA frees its tensor memory or leaves while the even CTA's MMAs may still read
+  // the odd CTA's shared memory or the odd CTA's roles still arrive on the even CTA's barriers
+  if constexpr (PAIR) tc_cluster_sync();
   if (warp == kTcMmaWarp) {
     __syncwarp();
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "n"(kTcTmemCols));
+    tc_dealloc<PAIR>(tmem);
   }
   if (*gave_up && tid == 0) {
     for (uint32_t q = 0; q < a.nq; q++) atomicOr(a.status + a.q0 + q, ST_DEVICE);

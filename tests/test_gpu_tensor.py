@@ -26,11 +26,16 @@ def run(eng, Q, k):
 
 # rows not a multiple of 128 (a partial last tile); cols covering one partial chunk (200),
 # a partial last chunk (500, 900) and four full chunks (1024); 130 queries = a full block and
-# a block of two; the three quantisers; one and 32 partitions; three chunk buffers, and two
-# where the thresholds of 32 partitions leave no room for a third (1024 columns)
+# a block of two, run by a CTA pair (two blocks per launch); 300 = a pair and a single block;
+# the three quantisers; one and 32 partitions; three chunk buffers, and two where the
+# thresholds of 32 partitions leave no room for a third (1024 columns); an odd number of row
+# tiles (the last pair's second CTA has none)
 @pytest.mark.parametrize("rows,cols,quant,split,ck,nq", [
     (20000, 1024, 0, 1, 1024, 130),
     (12000, 1024, 1, 32, 512, 40),
+    (12000, 1024, 1, 32, 512, 256),
+    (12800 + 77, 1024, 1, 1, 256, 300),
+    (9000, 500, 0, 4, 512, 256),
     (20000, 1024, 1, 1, 256, 128),
     (9000, 500, 2, 32, 512, 64),
     (7777, 200, 0, 32, 512, 20),
@@ -104,12 +109,14 @@ def test_tensor_layout_not_built_for_duplicates_or_wide_bits():
         assert e2.info()["tensor_tiles"] == 0
 
 
-def test_tensor_pass_gives_up_and_recovers():
+@pytest.mark.parametrize("nq", [64, 200])
+def test_tensor_pass_gives_up_and_recovers(nq):
     """The failure path of the pass's bounded waits: with the MMA role idle (a test flag) every
     hand-over wait of the producers and the epilogue runs out after about a second, the pass
     frees its tensor memory and the run returns AES_ERR_CUDA; the next ordinary run on the same
-    handle is oracle-exact, so the context and the tensor memory are usable again."""
-    rows, cols, k, ck, nq = 40000, 1024, 100, 256, 64  # 313 row tiles: every CTA has two or more
+    handle is oracle-exact, so the context and the tensor memory are usable again.  200 queries
+    run on CTA pairs: both CTAs of a pair give up and meet before they free tensor memory."""
+    rows, cols, k, ck = 40000, 1024, 100, 256  # 313 row tiles: every CTA has two or more
     ptr, col, val = E.gen_matrix(E.GEN_UNIFORM_DEG, rows, cols, 10, 30, seed=77)
     m = orc.Matrix(rows, cols, ptr, col, val, 4, orc.QUANT_UNSIGNED_ROW)
     eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=E.QUANT_UNSIGNED_ROW,
