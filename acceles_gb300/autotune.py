@@ -219,14 +219,16 @@ def main():
     eng.stats(reset=True)
     eng(k=args.k)
     stp = eng.stats(reset=True)
-    launch_ms = stp["cand_ms"] / max(stp["cand_timed"], 1)
+    launches = max(stp["cand_timed"], 1)
+    launch_ms = stp["cand_ms"] / launches
+    q_launch = nq / launches  # queries one launch scores (tensor cores: 256 on CTA pairs)
     kpad = (args.cols + 31) // 32 * 32
     rtiles = (args.rows + 127) // 128
     if tflag:
-        # tensor-core pass: 4-byte entries, chunk offsets, the e4m3 query operand; dense FP8
-        # products of every 128-row tile with the 128 queries
-        alg = info["quantized_nnz"] * 4 + (rtiles * ((kpad + 255) // 256) + 1) * 4 + 128 * kpad
-        flops = 2.0 * rtiles * 128 * 128 * kpad
+        # tensor-core pass: 4-byte entries, chunk offsets, the e4m3 query operands; dense FP8
+        # products of every 128-row tile with the launch's queries
+        alg = info["quantized_nnz"] * 4 + (rtiles * ((kpad + 255) // 256) + 1) * 4 + q_launch * kpad
+        flops = 2.0 * rtiles * 128 * q_launch * kpad
     else:
         alg = info["packets"] * 64 + (info["tiles"] + 1) * 4 + args.cols * (128 if prm["batch_tile"] == 128 else 1)
         flops = None
@@ -240,7 +242,8 @@ def main():
     emit({"workload": "batched sparse queries, 20Mx1024 gamma deg, 4-bit", "queries_per_step": nq,
           "steps": args.steps, "qps_device": qps_dev, "qps_e2e_host_buffers": qps_e2e,
           "ms_per_step_device": dev_ns / 1e6 / args.steps, "repaired": st["repaired"],
-          "cand_pass": {"launch_ms": launch_ms, "alg_bytes": alg, "gbs": gbs,
+          "cand_pass": {"launch_ms": launch_ms, "queries_per_launch": q_launch,
+                        "ms_per_128_queries": launch_ms * 128 / q_launch, "alg_bytes": alg, "gbs": gbs,
                         "frac_of_measured_hbm": gbs / peak, "tensor_cores": bool(tflag),
                         "dense_tflops": (flops / (launch_ms / 1e3) / 1e12) if flops else None,
                         "frac_of_fp8_dense": ((flops / (launch_ms / 1e3) / 1e12) / (2 * bf16))
