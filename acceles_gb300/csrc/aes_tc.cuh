@@ -246,7 +246,8 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 
 // Epilogue warps: reads accumulator `dbuf` of row tile T (thread = row, half the queries) and
 // appends every (row, query) key at or above the query's threshold.  thf holds the thresholds as
-// FP32 bounds: the score (an exact integer in FP32) or rowscale * score is compared directly.
+// FP32 bounds on rs * score: rs is the row's scale, or 1 without row scales (the score is an
+// exact integer in FP32, and times 1 it stays itself).
 // A block of 32 queries is compared without branches into a bit mask of hits.  The hits of a
 // thread then take their survivor slots with atomics issued back to back (none waits for
 // another's result) before any survivor is written, so a block costs one atomic round trip
@@ -280,7 +281,7 @@ __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         const float f = __uint_as_float(v[4 * j4 + u]);
-        hit |= ((a.rowscale ? __fmul_rn(f, rs) : f) >= tj[u] ? 1u : 0u) << (4 * j4 + u);
+        hit |= (__fmul_rn(f, rs) >= tj[u] ? 1u : 0u) << (4 * j4 + u);
       }
     }
     if (!valid || col0 >= a.nq) hit = 0;
@@ -492,7 +493,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
     for (uint32_t tl = 0; tl < ntl; tl++) {
       const uint32_t d = tl % ACC;
       const uint32_t T = tile_of(unit + tl * units), row = tc_epi_row(T);
-      const float rs = (a.rowscale && row < a.n_rows) ? __ldg(a.rowscale + row) : 0.0f;
+      // without row scales rs = 1: f * 1 is f exactly, so every score takes one path
+      const float rs = a.rowscale ? (row < a.n_rows ? __ldg(a.rowscale + row) : 0.0f) : 1.0f;
       ok &= tc_wait<PAIR>(b_full + 8u * d, (tl / ACC) & 1u, gave_up);
       ok = __all_sync(0xFFFFFFFFu, ok);  // tcgen05.ld needs the whole warp
       if (!ok) break;
