@@ -11,15 +11,18 @@
 // per tile of 128 consecutive rows, with the row tile A densified in shared memory:
 //   - the host lays out the quantised entries per (row tile, 256-column chunk) as 32-bit words
 //     holding the entry's byte offset inside the chunk's operand layout and its e4m3 byte;
-//   - producer warps write a chunk's entries into one of two zeroed 32 KB chunk buffers (and
-//     write them back to zero once the MMAs of that chunk have read the buffer);
+//   - producer warps write a chunk's entries into one of two or three zeroed 32 KB chunk buffers
+//     (and write them back to zero once the MMAs of that chunk have read the buffer);
 //   - one thread issues the chunk's tcgen05.mma (kind::f8f6f4, M = 128, N = 128, K = 32 each)
-//     into one of two 128-column FP32 accumulators in tensor memory; tcgen05.commit signals
+//     into one of four 128-column FP32 accumulators in tensor memory; tcgen05.commit signals
 //     mbarriers when a chunk buffer is read and when a tile's accumulator is complete;
-//   - epilogue warps read a complete accumulator with tcgen05.ld while the next tile's MMAs run:
+//   - epilogue warps read a complete accumulator with tcgen05.ld while the next tiles' MMAs run:
 //     every (row, query) score becomes the same candidate key as in the other passes and is
 //     compared with the query's threshold; hits are appended exactly as the dp4a pass appends
 //     them.
+// Two blocks of 128 queries run together on CTA pairs (cta_group::2, M = 256 over the pair's two
+// row tiles, N = 256 queries): the same roles in each CTA, the even CTA's thread issuing the MMAs
+// (see k_cand_tc).
 // The roles hand work over through mbarriers only.
 // Both operands are K-major without swizzle (layout in aes_tc_layout.h).
 // Reference counterpart: the candidate pass spmv_ucsr_top_k_multicore.hpp:195-413 (one query per
@@ -33,9 +36,10 @@ namespace aes {
 namespace dev {
 
 // Warp roles: warps 0-7 stage the chunks (producers), warps 8-15 read the accumulators (warp w
-// may only read tensor-memory lanes 32 (w % 4) .. + 31; warps 8-11 take queries 0-63, warps
-// 12-15 queries 64-127), warp 16 allocates tensor memory and its lane 0 issues the MMAs.  They
-// hand work over through mbarriers only.
+// may only read tensor-memory lanes 32 (w % 4) .. + 31; warps 8-11 take the first half of the
+// queries, warps 12-15 the second), warp 16 allocates tensor memory and its lane 0 issues the
+// MMAs (on a pair: the even CTA's; lanes 0 and 1 of the odd CTA's forward barrier phases).
+// They hand work over through mbarriers only.
 constexpr int kTcProducers = 256;
 constexpr int kTcEpiWarp = 8;
 constexpr int kTcEpilogue = 256;
