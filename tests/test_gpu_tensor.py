@@ -29,13 +29,14 @@ def run(eng, Q, k):
 # a block of two, run by a CTA pair (two blocks per launch); 300 = a pair and a single block;
 # the three quantisers; one and 32 partitions; three chunk buffers, and two where the
 # thresholds of 32 partitions leave no room for a third (1024 columns); an odd number of row
-# tiles (the last pair's second CTA has none)
+# tiles (the last pair's second CTA has none); a matrix of one row tile on a pair
 @pytest.mark.parametrize("rows,cols,quant,split,ck,nq", [
     (20000, 1024, 0, 1, 1024, 130),
     (12000, 1024, 1, 32, 512, 40),
     (12000, 1024, 1, 32, 512, 256),
     (12800 + 77, 1024, 1, 1, 256, 300),
     (9000, 500, 0, 4, 512, 256),
+    (100, 64, 1, 1, 64, 200),
     (20000, 1024, 1, 1, 256, 128),
     (9000, 500, 2, 32, 512, 64),
     (7777, 200, 0, 32, 512, 20),
@@ -133,3 +134,25 @@ def test_tensor_pass_gives_up_and_recovers(nq):
     for i in (0, nq - 1):
         oi, os_, _ = m.two_stage(Q[i], 1, ck, k)
         assert np.array_equal(idx[i, :len(oi)], oi) and np.array_equal(sc[i, :len(oi)], os_)
+
+
+def test_tensor_pass_graph_replay_on_pairs():
+    """A CUDA graph captured with the pair launches (clusters of two CTAs) replays to the same
+    results as direct launches, for a batch of two blocks and one of three (a pair and a single
+    CTA)."""
+    rows, cols, k = 30000, 1024, 100
+    ptr, col, val = E.gen_matrix(E.GEN_GAMMA_DEG, rows, cols, 32, 512, seed=91)
+    for nq in (256, 300):
+        Q = queries(cols, nq, 92, signed=False)
+        out = []
+        for flags in (E.FLAG_TENSOR, E.FLAG_TENSOR | E.FLAG_GRAPHS):
+            eng = E.SpMV(rows, cols, ptr=ptr, col=col, val=val, bits=4, quant=E.QUANT_UNSIGNED_ROW,
+                         split=1, ck=256, k_max=k, max_batch=nq, batch_tile=128, flags=flags)
+            assert eng.info()["tensor_tiles"] == 1
+            for _ in range(2):  # with graphs: capture, then replay
+                eng.Q_reset(Q)
+                eng(k=k)
+                out.append(tuple(x.copy() for x in eng.read_topk()))
+            eng.close()
+        for o in out[1:]:
+            assert np.array_equal(o[0], out[0][0]) and np.array_equal(o[1], out[0][1])
