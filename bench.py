@@ -130,13 +130,13 @@ def tensor_4bit_leg(local, steps=5, warmup=3):
         eng(k=k)
         st = eng.stats(reset=True)
         # the pass's device time of one step over its blocks of 128 queries (the tensor-core
-        # pass launches once per block, the dp4a pass once for every block)
+        # pass launches once per two blocks, on CTA pairs; the dp4a pass once for all blocks)
         out[name] = {"queries_per_s": steps * nq / (ns / 1e9),
                      "ms_per_step": ns / 1e6 / steps,
                      "pass_ms_per_128_queries": st["cand_ms"] / (nq // 128),
                      "pass_launches_timed": int(st["cand_timed"]),
                      "repaired_queries": int(st["repaired"])}
-    # dense FP8 products of one launch: every 128-row tile times the 128-query operand
+    # dense FP8 products per 128 queries: every 128-row tile times a 128-query operand
     flops = 2.0 * ((rows + 127) // 128) * 128 * 128 * 1024
     tc = out["tensor_cores"]
     tc["dense_tflops"] = flops / (tc["pass_ms_per_128_queries"] / 1e3) / 1e12
