@@ -262,10 +262,12 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 __device__ __forceinline__ uint32_t tc_epi_row(uint32_t T) {
   return T * kTcRows + ((threadIdx.x >> 5) & 3u) * 32u + (threadIdx.x & 31u);
 }
+// The accumulator goes back to the MMA role (an arrive on `empty`) as soon as the thread's last
+// load from it has completed, so the compares of the last block overlap the next MMAs.
 template <bool PAIR>
 __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_t tmem,
                                             uint32_t dbuf, const float* thf_all, uint32_t S,
-                                            float rs) {
+                                            float rs, uint32_t empty) {
   constexpr uint32_t Q = TcShape<PAIR>::Q, HALF = Q / 2;
   const uint32_t warp = threadIdx.x >> 5;
   const uint32_t g = warp & 3u, h = (warp - kTcEpiWarp) >> 2;
@@ -277,6 +279,10 @@ __device__ __forceinline__ void tc_epilogue(const TcArgs& a, uint32_t T, uint32_
   for (uint32_t col0 = h * HALF; col0 < h * HALF + HALF; col0 += 32u) {
     uint32_t v[32];
     tc_ld32(tmem + dbuf * Q + col0 + ((g * 32u) << 16), v);
+    if (col0 + 32u == h * HALF + HALF) {  // the last load of this unit has completed
+      tc_fence_before();
+      tc_arrive(empty);
+    }
     uint32_t hit = 0;
 #pragma unroll
     for (int j4 = 0; j4 < 8; j4++) {  // the same 32 thresholds for every lane: 16-byte broadcasts
@@ -503,9 +509,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cand_tc(TcArgs a) {
       ok = __all_sync(0xFFFFFFFFu, ok);  // tcgen05.ld needs the whole warp
       if (!ok) break;
       tc_fence_after();
-      tc_epilogue<PAIR>(a, T, tmem, d, thf, S, rs);
-      tc_fence_before();
-      tc_arrive(b_empty + 8u * d);
+      tc_epilogue<PAIR>(a, T, tmem, d, thf, S, rs, b_empty + 8u * d);
     }
   } else if ((tid & 31u) == 0 && rank == 0) {
     // ---- MMA issue (one thread; PAIR: of the even CTA) ----------------------------------------
