@@ -234,7 +234,13 @@ struct PacketSpans {
     else return window32<480>(w) >> (POS - 480);
   }
 
-  // the four B-bit values at the bottom of x as bytes in element order (sign-extended when SGN)
+  // Scores of signed 6-bit packets come out four times too large: their values sit at bits 2-7
+  // of each byte (unpack), where the byte's sign is the value's, so no sign extension is needed;
+  // sums of them are exact multiples of four, shifted back where a row's score is emitted.
+  static constexpr int kScoreShift = (B == 6 && SGN) ? 2 : 0;
+
+  // the four B-bit values at the bottom of x as bytes in element order (sign-extended when SGN;
+  // signed 6-bit: four times each value)
   __device__ __forceinline__ static uint32_t unpack(uint32_t x) {
     if constexpr (B == 8) {
       return x;
@@ -243,12 +249,17 @@ struct PacketSpans {
       uint32_t v = (z | (z * 16u)) & 0x0F0F0F0Fu;
       if constexpr (SGN) v |= (v & 0x08080808u) * 0x1Eu;  // bit 3 -> bits 4..7 of each byte
       return v;
+    } else if constexpr (SGN) {
+      static_assert(B == 6, "bit width");
+      // bits 0-11 of h are values 0 and 1, bits 16-27 values 2 and 3 (bits 12-15 and 28-31 are
+      // never selected below); value k then goes to bits 8k + 2 .. 8k + 7
+      const uint32_t x16 = x * 16u;
+      const uint32_t h = (x & 0xFFFu) | (x16 & 0xFFFFF000u);
+      return ((h * 4u) & 0x00FC00FCu) | ((h * 16u) & 0xFC00FC00u);
     } else {
       static_assert(B == 6, "bit width");
       const uint32_t h = (x & 0xFFFu) | ((x * 16u) & 0x0FFF0000u);      // 12-bit halves
-      uint32_t v = (h & 0x003F003Fu) | ((h * 4u) & 0x3F003F00u);        // 6-bit bytes
-      if constexpr (SGN) v |= (v & 0x20202020u) * 6u;  // bit 5 -> bits 6..7 of each byte
-      return v;
+      return (h & 0x003F003Fu) | ((h * 4u) & 0x3F003F00u);              // 6-bit bytes
     }
   }
 
@@ -404,7 +415,8 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t,
   const uint32_t lane = threadIdx.x & 31u;
   if constexpr (CLOSING) {
     if (t >= a.n_tiles) {  // the end of the matrix closes the last row
-      if (st.open_owned && lane == 0) emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG));
+      if (st.open_owned && lane == 0)
+        emit(a.n_rows - 1, (int32_t)(st.carryG - st.startG) >> D::kScoreShift);
       return true;
     }
   }
@@ -427,7 +439,8 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t,
       ts = r1 < pt.end ? pt.ts : emit.score_bound(rowbase, r1);
     }
   }
-  auto on_row = [&](bool valid, uint32_t row, int32_t sc) {
+  auto on_row = [&](bool valid, uint32_t row, int32_t sc4) {
+    const int32_t sc = sc4 >> D::kScoreShift;
     if constexpr (KIND == EMIT_INT_ONE) {
       if (valid && sc >= ts) emit.append_int(row, sc);
     } else if constexpr (KIND == EMIT_INT_PARTS) {
@@ -449,7 +462,7 @@ __device__ __forceinline__ bool tile_step(const PlainArgs& a, uint32_t t,
       return false;
     }
     if (lane == (uint32_t)(__ffs(has_mask) - 1) && st.open_owned)
-      emit(rowbase, (int32_t)(LB + s.first - st.startG));
+      emit(rowbase, (int32_t)(LB + s.first - st.startG) >> D::kScoreShift);
     return true;
   } else {
     // the row closed by a lane's first flag started at the last flag of the lanes before it,
