@@ -322,6 +322,10 @@ def check_vs_oracle(m, Q, idx, score, split, nthreads):
             "max_rel_err_vs_fp64": float(rel.max()) if rel.size else 0.0}
 
 
+SMALL_METRIC = ("Top-100 queries/s, 400k×500 |N(0,1)| 69 nnz/row, 6-bit, SPLIT=32, CK=512 "
+                "(plain method, small)")
+
+
 def run_small(args, rank, world):
     """The reference's small plain-method configuration: 400,000 x 500 at 69 distinct uniform
     columns per row, FP32 values |N(0,1)|, the reference's global 6-bit quantiser, SPLIT=32,

@@ -62,3 +62,15 @@ def test_reference_arm_loads_only_the_oracle():
     line = d["line"]
     assert line["impl"] == "reference" and line["steps"] == 2 and line["ms_per_step"] > 0
     assert line["config"] == bench.headline_config(20000, line["config"]["nnz"], 1, 4096)
+
+
+def test_every_workload_names_its_metric():
+    """Each --workload leg prints a line with its own metric name (defined at module level)."""
+    for name in ("METRIC", "SMALL_METRIC", "SERVE_METRIC"):
+        assert isinstance(getattr(bench, name), str) and getattr(bench, name)
+    import ast
+    tree = ast.parse(open(bench.__file__).read())
+    defined = {t.id for n in ast.walk(tree) if isinstance(n, ast.Assign) for t in n.targets
+               if isinstance(t, ast.Name)}
+    used = {n.id for n in ast.walk(tree) if isinstance(n, ast.Name) and n.id.endswith("METRIC")}
+    assert used <= defined, used - defined
