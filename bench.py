@@ -413,7 +413,7 @@ SERVE_METRIC = ("served queries/s with p50/p99 latency under Poisson arrivals, t
 
 
 def run_serve(args, rank, world):
-    """The serving workload: three device-resident 8-bit matrices, two batch slots each (the
+    """The serving workload: three device-resident 8-bit matrices, --serve-slots batch slots each (the
     handle and a view), Poisson arrivals at each offered rate for --serve-seconds, every request
     picking a matrix and K uniformly.  `value` is the served rate at the highest offered rate."""
     if rank != 0:
@@ -422,7 +422,7 @@ def run_serve(args, rank, world):
     from acceles_gb300 import engine as E
     from acceles_gb300 import serve as S
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    srv = S.Server(slots=2)
+    srv = S.Server(slots=args.serve_slots)
     cols_of, mats = {}, []
     for name, kind, rows, cols, p0, p1, seed in S.serving_specs():
         ptr, col, val = E.gen_matrix(kind, rows, cols, p0, p1, seed=seed)
@@ -454,7 +454,8 @@ def run_serve(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded; reference matrices not shipped)",
             "config": {"workload": "serving: 3 resident matrices, Poisson arrivals, K in {8,32,100}, "
-                                   "8-bit, CK=1024, split=1, max batch 256, 2 batch slots per matrix",
+                                   f"8-bit, CK=1024, split=1, max batch 256, {args.serve_slots} batch slots "
+                                   "per matrix",
                        "matrices": mats, "offered_rates": rates, "seconds_per_rate": args.serve_seconds},
             "legs": legs, "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
             "max_batches_in_flight_per_matrix": in_flight, "clocks": clk,
@@ -489,6 +490,8 @@ def main():
     ap.add_argument("--serve-rates", default="1000,10000,50000",
                     help="offered queries/s of the serving workload")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-slots", type=int, default=2,
+                    help="batch slots per matrix (the owning handle and views of it)")
     ap.add_argument("--split", type=int, default=1,
                     help="row partitions with a Top-(CK/split) each (the reference default is 32)")
     ap.add_argument("--bits", type=int, default=8, choices=[4, 6, 8],
