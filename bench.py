@@ -413,8 +413,8 @@ SERVE_METRIC = ("served queries/s with p50/p99 latency under Poisson arrivals, t
 
 
 def run_serve(args, rank, world):
-    """The serving workload: three device-resident 8-bit matrices, --serve-slots batch slots each (the
-    handle and a view), Poisson arrivals at each offered rate for --serve-seconds, every request
+    """The serving workload: three device-resident 8-bit matrices, --serve-slots batch slots each
+    (the handle and views of it), Poisson arrivals at each offered rate for --serve-seconds, every request
     picking a matrix and K uniformly.  `value` is the served rate at the highest offered rate."""
     if rank != 0:
         return
